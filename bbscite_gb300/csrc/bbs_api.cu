@@ -1,0 +1,1029 @@
+// bbs_api.cu -- the C ABI (include/bbscite_gb300.h): contexts, argument
+// checks, host tree helpers and the SCITE input format.  Every entry point
+// catches everything and returns a status; nothing aborts across the ABI.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "bbs_internal.h"
+
+using namespace bbs;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+int cuda_fail(int err, const char *what) {
+  return fail(BBS_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString((cudaError_t)err));
+}
+
+#define BBS_CUDA(call, what)                                   \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return cuda_fail((int)e_, (what));  \
+  } while (0)
+
+inline uint32_t words64(uint32_t n) { return (n + 63u) / 64u; }
+inline bool getb(const uint64_t *row, uint32_t i) {
+  return (row[i >> 6] >> (i & 63u)) & 1u;
+}
+inline void setb(uint64_t *row, uint32_t i) { row[i >> 6] |= 1ull << (i & 63u); }
+
+// Host Philox4x32-10 (same algorithm as the device sampler).
+void philox(const uint32_t c_in[4], const uint32_t k_in[2], uint32_t out[4]) {
+  uint32_t c0 = c_in[0], c1 = c_in[1], c2 = c_in[2], c3 = c_in[3];
+  uint32_t k0 = k_in[0], k1 = k_in[1];
+  for (int r = 0; r < 10; r++) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    c0 = n0;
+    c1 = (uint32_t)p1;
+    c2 = n2;
+    c3 = (uint32_t)p0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+// Parent vector checks: entries < n, root (n-1) is its own parent, every
+// node reaches the root.
+int check_parent_vector(const uint32_t *pv, uint32_t n) {
+  if (n < 2) return fail(BBS_ERR_INPUT, "a tree needs at least 2 nodes");
+  if (pv[n - 1] != n - 1)
+    return fail(BBS_ERR_INPUT, "the root %u must be its own parent", n - 1);
+  for (uint32_t x = 0; x < n; x++) {
+    if (pv[x] >= n)
+      return fail(BBS_ERR_INPUT, "parent of node %u is %u >= %u", x, pv[x], n);
+    uint32_t y = x, steps = 0;
+    while (y != n - 1) {
+      y = pv[y];
+      if (++steps > n)
+        return fail(BBS_ERR_INPUT, "the parent vector has a cycle at node %u", x);
+    }
+  }
+  return BBS_OK;
+}
+
+// src/MutationTree.hpp:379-409 (after check_parent_vector).
+void parent_to_matrix(const uint32_t *pv, uint32_t n, uint64_t *am,
+                      uint64_t *dm) {
+  const uint32_t W = words64(n), root = n - 1;
+  if (am) std::memset(am, 0, sizeof(uint64_t) * W * n);
+  if (dm) std::memset(dm, 0, sizeof(uint64_t) * W * n);
+  for (uint32_t i = 0; i < n; i++) {
+    uint32_t anc = i;
+    while (anc != root) {
+      if (am) setb(am + (size_t)anc * W, i);
+      if (dm) setb(dm + (size_t)i * W, anc);
+      anc = pv[anc];
+    }
+    if (am) {
+      setb(am + (size_t)i * W, i);
+      setb(am + (size_t)root * W, i);
+    }
+    if (dm) {
+      setb(dm + (size_t)i * W, i);
+      setb(dm + (size_t)i * W, root);
+    }
+  }
+}
+
+// Parent = the deepest proper ancestor; the root is its own parent.
+void matrix_to_parent(const uint64_t *dm, uint32_t n, uint32_t *pv) {
+  const uint32_t W = words64(n);
+  std::vector<int> depth(n);
+  for (uint32_t x = 0; x < n; x++) {
+    int d = 0;
+    for (uint32_t k = 0; k < W; k++) d += __builtin_popcountll(dm[x * W + k]);
+    depth[x] = d;
+  }
+  for (uint32_t x = 0; x < n; x++) {
+    uint32_t best = x;
+    int bd = -1;
+    for (uint32_t y = 0; y < n; y++)
+      if (y != x && getb(dm + (size_t)x * W, y) && depth[y] > bd) {
+        bd = depth[y];
+        best = y;
+      }
+    pv[x] = best;
+  }
+}
+
+void pruefer_decode(const uint32_t *code, uint32_t len, uint32_t *parent) {
+  const uint32_t n = len + 2;
+  std::vector<uint32_t> degree(n, 1);
+  for (uint32_t i = 0; i < n; i++) parent[i] = n - 1;
+  for (uint32_t i = 0; i < len; i++) degree[code[i]]++;
+  // The smallest degree-1 node each step (src/MutationTree.hpp:454-463).
+  std::vector<uint32_t> heap;
+  for (uint32_t j = 0; j < n; j++)
+    if (degree[j] == 1) heap.push_back(j);
+  std::make_heap(heap.begin(), heap.end(), std::greater<uint32_t>());
+  for (uint32_t i = 0; i < len; i++) {
+    std::pop_heap(heap.begin(), heap.end(), std::greater<uint32_t>());
+    const uint32_t j = heap.back();
+    heap.pop_back();
+    parent[j] = code[i];
+    degree[code[i]]--;
+    degree[j]--;
+    if (degree[code[i]] == 1) {
+      heap.push_back(code[i]);
+      std::push_heap(heap.begin(), heap.end(), std::greater<uint32_t>());
+    }
+  }
+  for (uint32_t i = 0; i < n; i++)
+    if (degree[i] == 1) {
+      parent[i] = n - 1;
+      break;
+    }
+}
+
+void random_parents(uint64_t seed, uint32_t n_genes, uint32_t n_trees,
+                    uint32_t *out) {
+  const uint32_t n = n_genes + 1;
+  std::vector<uint32_t> code(n >= 2 ? n - 2 : 0);
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (uint32_t t = 0; t < n_trees; t++) {
+    for (uint32_t i = 0; i < code.size(); i += 4) {
+      const uint32_t ctr[4] = {i, t, 0x7265u /* tree stream */, 0u};
+      uint32_t r[4];
+      philox(ctr, key, r);
+      for (uint32_t k = 0; k < 4 && i + k < code.size(); k++)
+        code[i + k] = (uint32_t)(((uint64_t)r[k] * n) >> 32);
+    }
+    pruefer_decode(code.data(), (uint32_t)code.size(), out + (size_t)t * n);
+  }
+}
+
+void newick_rec(const std::vector<std::vector<uint32_t>> &ch, uint32_t x,
+                std::string &s) {
+  if (!ch[x].empty()) {
+    s += '(';
+    for (size_t i = 0; i < ch[x].size(); i++) {
+      newick_rec(ch, ch[x][i], s);
+      if (i + 1 != ch[x].size()) s += ',';
+    }
+    s += ')';
+  }
+  s += std::to_string(x);
+}
+
+int put_string(const std::string &s, char *buf, size_t cap, size_t *len) {
+  if (len) *len = s.size();
+  if (buf && cap > 0) {
+    const size_t k = std::min(cap - 1, s.size());
+    std::memcpy(buf, s.data(), k);
+    buf[k] = '\0';
+  }
+  return BBS_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------
+// Context
+// ------------------------------------------------------------------------
+struct bbs_ctx {
+  int device = 0, n_sms = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t n_cells = 0, n_genes = 0, n_nodes = 0, W64 = 0, RS = 0;
+  bbs_params params{};
+  DatasetDev ds{};
+  MoveProbs mp{};
+  float l01_0 = 0, l11_0 = 0, prior_0 = 0;  // terms of beta_mean (host libm)
+  uint32_t *d_K = nullptr, *d_M = nullptr;
+  uint32_t n_chains = 0;
+  uint32_t *d_rows = nullptr, *d_best = nullptr;
+  ChainState *d_states = nullptr;
+  int *d_status = nullptr;
+  int *h_cancel = nullptr;        // mapped pinned flag
+  int *d_cancel = nullptr;
+  int q = 1, wpb = 1;
+  bool running = false;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.0f;
+};
+
+namespace {
+
+void free_chains(bbs_ctx *c) {
+  cudaFree(c->d_rows);
+  cudaFree(c->d_best);
+  cudaFree(c->d_states);
+  c->d_rows = c->d_best = nullptr;
+  c->d_states = nullptr;
+  c->n_chains = 0;
+}
+
+// Host values of the beta-dependent log-table entries and logscore_beta,
+// exactly as src/TreeScorer.hpp:104-106, 122-126, 136-137 compute them.
+void host_beta_terms(const DatasetDev &ds, float beta, float *l01, float *l11,
+                     float *prior) {
+  *l01 = logf(beta);
+  *l11 = (float)std::log(1.0 - (double)beta);
+  float r = ds.lg_ab;
+  r = r + (ds.bpa - 1.0f) * logf(beta);
+  r = r + (ds.bpb - 1.0f) * logf(1.0f - beta);
+  r = r - ds.lg_a;
+  r = r - ds.lg_b;
+  *prior = r;
+}
+
+int check_params(const bbs_params *p) {
+  if (!p) return fail(BBS_ERR_INPUT, "params is NULL");
+  const float probs[4] = {p->prob_beta_change, p->prob_prune_n_reattach,
+                          p->prob_swap_nodes, p->prob_swap_subtrees};
+  for (float v : probs)
+    if (!(v >= 0.0f)) return fail(BBS_ERR_INPUT, "Move probabilities may not be negative.");
+  if (probs[0] + probs[1] + probs[2] + probs[3] == 0.0f)
+    return fail(BBS_ERR_INPUT, "The sum of the move type probabilities is zero.");
+  if (!(p->alpha_mean > 0.0f && p->alpha_mean < 1.0f))
+    return fail(BBS_ERR_INPUT, "alpha must lie in (0, 1), got %g", p->alpha_mean);
+  if (!(p->beta_mean > 0.0f && p->beta_mean < 1.0f))
+    return fail(BBS_ERR_INPUT, "beta must lie in (0, 1), got %g", p->beta_mean);
+  if (!(p->beta_sd > 0.0f)) return fail(BBS_ERR_INPUT, "beta_sd must be positive");
+  return BBS_OK;
+}
+
+int sync_stream(bbs_ctx *c, const char *what) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_fail((int)e, what);
+  return BBS_OK;
+}
+
+template <typename T>
+struct DevBuf {
+  T *p = nullptr;
+  ~DevBuf() { cudaFree(p); }
+  cudaError_t alloc(size_t n) { return cudaMalloc((void **)&p, sizeof(T) * std::max<size_t>(n, 1)); }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char *bbs_last_error(void) { return g_error.c_str(); }
+const char *bbs_version(void) { return "bbscite_gb300 0.1 (sm_103a)"; }
+uint32_t bbs_words(uint32_t n_nodes) { return words64(n_nodes); }
+
+void bbs_params_default(bbs_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->alpha_mean = 6.04e-5f;
+  p->beta_mean = 0.4309f;
+  p->beta_sd = 0.1f;
+  p->prob_beta_change = 0.0f;
+  p->prob_prune_n_reattach = 0.55f;
+  p->prob_swap_nodes = 0.4f;
+  p->prob_swap_subtrees = 0.05f;
+  p->beta_jump_scaling_chi = 10.0f;
+  p->gamma = 1.0f;
+  p->seed = 0x5eed5eedull;
+}
+
+int bbs_pruefer_to_parent_vector(const uint32_t *code, uint32_t code_len,
+                                 uint32_t *parent) {
+  if (!parent || (code_len && !code)) return fail(BBS_ERR_INPUT, "NULL buffer");
+  if (code_len + 2 > BBS_MAX_GENES + 1)
+    return fail(BBS_ERR_SIZE, "at most %d nodes", BBS_MAX_GENES + 1);
+  for (uint32_t i = 0; i < code_len; i++)
+    if (code[i] >= code_len + 2)
+      return fail(BBS_ERR_INPUT, "code entry %u out of range", code[i]);
+  pruefer_decode(code, code_len, parent);
+  return BBS_OK;
+}
+
+int bbs_parent_vector_to_matrix(const uint32_t *parent, uint32_t n_nodes,
+                                uint64_t *am, uint64_t *dm) {
+  if (!parent) return fail(BBS_ERR_INPUT, "NULL parent vector");
+  if (n_nodes > BBS_MAX_GENES + 1) return fail(BBS_ERR_SIZE, "too many nodes");
+  const int r = check_parent_vector(parent, n_nodes);
+  if (r != BBS_OK) return r;
+  parent_to_matrix(parent, n_nodes, am, dm);
+  return BBS_OK;
+}
+
+int bbs_matrix_to_parent_vector(const uint64_t *dm, uint32_t n_nodes,
+                                uint32_t *parent) {
+  if (!dm || !parent) return fail(BBS_ERR_INPUT, "NULL buffer");
+  if (n_nodes < 1 || n_nodes > BBS_MAX_GENES + 1)
+    return fail(BBS_ERR_SIZE, "node count %u out of range", n_nodes);
+  matrix_to_parent(dm, n_nodes, parent);
+  return BBS_OK;
+}
+
+int bbs_dm_to_am(const uint64_t *dm, uint32_t n_nodes, uint64_t *am) {
+  if (!dm || !am) return fail(BBS_ERR_INPUT, "NULL buffer");
+  const uint32_t W = words64(n_nodes);
+  std::memset(am, 0, sizeof(uint64_t) * W * n_nodes);
+  for (uint32_t x = 0; x < n_nodes; x++)
+    for (uint32_t y = 0; y < n_nodes; y++)
+      if (getb(dm + (size_t)x * W, y)) setb(am + (size_t)y * W, x);
+  return BBS_OK;
+}
+
+int bbs_tree_to_graphviz(const uint32_t *parent, uint32_t n_nodes, char *buf,
+                         size_t cap, size_t *len) {
+  if (!parent) return fail(BBS_ERR_INPUT, "NULL parent vector");
+  std::string s = "digraph G {\nnode [color=deeppink4, style=filled, fontcolor=white];\n";
+  for (uint32_t x = 0; x + 1 < n_nodes; x++)
+    s += std::to_string(parent[x]) + " -> " + std::to_string(x) + ";\n";
+  s += "}\n";
+  return put_string(s, buf, cap, len);
+}
+
+int bbs_tree_to_newick(const uint32_t *parent, uint32_t n_nodes, char *buf,
+                       size_t cap, size_t *len) {
+  if (!parent) return fail(BBS_ERR_INPUT, "NULL parent vector");
+  const int r = check_parent_vector(parent, n_nodes);
+  if (r != BBS_OK) return r;
+  std::vector<std::vector<uint32_t>> ch(n_nodes);
+  for (uint32_t x = 0; x + 1 < n_nodes; x++) ch[parent[x]].push_back(x);
+  std::string s;
+  newick_rec(ch, n_nodes - 1, s);
+  s += '\n';
+  return put_string(s, buf, cap, len);
+}
+
+int bbs_random_parent_vectors(uint64_t seed, uint32_t n_genes,
+                              uint32_t n_trees, uint32_t *parents) {
+  if (!parents) return fail(BBS_ERR_INPUT, "NULL buffer");
+  if (n_genes < 1 || n_genes > BBS_MAX_GENES)
+    return fail(BBS_ERR_SIZE, "gene count %u out of range", n_genes);
+  random_parents(seed, n_genes, n_trees, parents);
+  return BBS_OK;
+}
+
+// src/main.cpp:50-144: first pass counts cells per line and lines, second
+// pass reads the entries.
+int bbs_read_csv(const char *path, uint32_t *n_cells, uint32_t *n_genes,
+                 uint64_t *is_mutated, uint64_t *is_known) {
+  if (!path || !n_cells || !n_genes) return fail(BBS_ERR_INPUT, "NULL argument");
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return fail(BBS_ERR_IO, "Error: could not open the input file %s", path);
+  uint32_t cells = 0, genes = 0, in_line = 0;
+  int ch;
+  while ((ch = in.get()) != EOF) {
+    const char c = (char)ch;
+    if (c == '0' || c == '1' || c == '2' || c == '3') {
+      in_line++;
+    } else if (c == '\n') {
+      if (cells == 0) {
+        cells = in_line;
+      } else if (cells != in_line) {
+        return fail(BBS_ERR_INPUT, "Error: Inconsistent rows in the input file!");
+      }
+      genes++;
+      in_line = 0;
+    } else if (c == ' ') {
+      continue;
+    } else {
+      return fail(BBS_ERR_INPUT, "Error: Illegal character %c in the input file!", c);
+    }
+  }
+  if (in_line == cells) {
+    genes++;
+  } else if (in_line != 0) {
+    return fail(BBS_ERR_INPUT, "Error: Inconsistent rows in the input file!");
+  }
+  if (cells == 0 || genes == 0) return fail(BBS_ERR_INPUT, "Error: Empty input file!");
+  if (cells > BBS_MAX_CELLS)
+    return fail(BBS_ERR_SIZE,
+                "Error: This build of bbSCITE only supports up %u cells. The "
+                "input data contains %u cells.",
+                (unsigned)BBS_MAX_CELLS, cells);
+  if (genes > BBS_MAX_GENES)
+    return fail(BBS_ERR_SIZE,
+                "Error: This build of bbSCITE only supports up %u genes. The "
+                "input data contains %u genes.",
+                (unsigned)BBS_MAX_GENES, genes);
+  *n_cells = cells;
+  *n_genes = genes;
+  if (!is_mutated || !is_known) return BBS_OK;
+  const uint32_t W = words64(genes + 1);
+  std::memset(is_mutated, 0, sizeof(uint64_t) * W * cells);
+  std::memset(is_known, 0, sizeof(uint64_t) * W * cells);
+  in.clear();
+  in.seekg(0);
+  for (uint32_t g = 0; g < genes; g++)
+    for (uint32_t c = 0; c < cells; c++) {
+      int entry = -1;
+      if (!(in >> entry))
+        return fail(BBS_ERR_INPUT, "Error: The input file contains the invalid entry %d", entry);
+      switch (entry) {
+        case 0: setb(is_known + (size_t)c * W, g); break;
+        case 1:
+        case 2:
+          setb(is_known + (size_t)c * W, g);
+          setb(is_mutated + (size_t)c * W, g);
+          break;
+        case 3: break;
+        default:
+          return fail(BBS_ERR_INPUT, "Error: The input file contains the invalid entry %d", entry);
+      }
+    }
+  return BBS_OK;
+}
+
+int bbs_create(bbs_ctx **out, const uint64_t *is_mutated,
+               const uint64_t *is_known, uint32_t n_cells, uint32_t n_genes,
+               const bbs_params *params) {
+  try {
+    if (!out || !is_mutated || !is_known)
+      return fail(BBS_ERR_INPUT, "NULL argument to bbs_create");
+    *out = nullptr;
+    if (n_genes < 2 || n_genes > BBS_MAX_GENES)
+      return fail(BBS_ERR_SIZE, "gene count %u outside [2, %d]", n_genes, BBS_MAX_GENES);
+    if (n_cells < 1 || n_cells > BBS_MAX_CELLS)
+      return fail(BBS_ERR_SIZE, "cell count %u outside [1, %d]", n_cells, BBS_MAX_CELLS);
+    int r = check_params(params);
+    if (r != BBS_OK) return r;
+    int n_dev = 0;
+    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
+      return fail(BBS_ERR_CUDA, "no CUDA device is available");
+    bbs_ctx *c = new (std::nothrow) bbs_ctx();
+    if (!c) return fail(BBS_ERR_ALLOC, "out of host memory");
+    c->params = *params;
+    c->n_cells = n_cells;
+    c->n_genes = n_genes;
+    c->n_nodes = n_genes + 1;
+    c->W64 = words64(c->n_nodes);
+    c->RS = 2 * c->W64;
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, c->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    // Cell rows: genes only (bits >= n_genes cleared), mutated within known.
+    std::vector<uint64_t> K((size_t)n_cells * c->W64), M(K.size());
+    int64_t sum_k = 0, sum_m = 0;
+    for (uint32_t cell = 0; cell < n_cells; cell++)
+      for (uint32_t k = 0; k < c->W64; k++) {
+        uint64_t mask = ~0ull;
+        const uint32_t lo = 64 * k;
+        if (lo >= n_genes) mask = 0;
+        else if (n_genes - lo < 64) mask = (1ull << (n_genes - lo)) - 1ull;
+        const size_t i = (size_t)cell * c->W64 + k;
+        K[i] = is_known[i] & mask;
+        M[i] = is_mutated[i] & K[i];
+        sum_k += __builtin_popcountll(K[i]);
+        sum_m += __builtin_popcountll(M[i]);
+      }
+    const size_t bytes = sizeof(uint64_t) * K.size();
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_K, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_M, bytes);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_K, K.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_M, M.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaHostAlloc(&c->h_cancel, sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+      *c->h_cancel = 0;
+      e = cudaHostGetDevicePointer((void **)&c->d_cancel, c->h_cancel, 0);
+    }
+    if (e != cudaSuccess) {
+      const int rr = cuda_fail((int)e, "bbs_create");
+      bbs_destroy(c);
+      return rr;
+    }
+    // src/TreeScorer.hpp:99-111
+    const float alpha = params->alpha_mean, bm = params->beta_mean, sd = params->beta_sd;
+    DatasetDev &ds = c->ds;
+    ds.K = c->d_K;
+    ds.M = c->d_M;
+    ds.n_cells = (int)n_cells;
+    ds.n_nodes = (int)c->n_nodes;
+    ds.sum_k = (int)sum_k;
+    ds.sum_m = (int)sum_m;
+    ds.l00 = (float)std::log(1.0 - (double)alpha);
+    ds.l10 = logf(alpha);
+    ds.bpa = (float)(((double)(1.0f - bm) * std::pow((double)bm, 2.0) /
+                      std::pow((double)sd, 2.0)) - (double)bm);
+    ds.bpb = ds.bpa * ((1.0f / bm) - 1.0f);
+    ds.lg_ab = logf(tgammaf(ds.bpa + ds.bpb));
+    ds.lg_a = logf(tgammaf(ds.bpa));
+    ds.lg_b = logf(tgammaf(ds.bpb));
+    host_beta_terms(ds, bm, &c->l01_0, &c->l11_0, &c->prior_0);
+    // src/Parameters.hpp:451-584, src/RawMoveDistribution.hpp:119-131
+    const float sum = params->prob_beta_change + params->prob_prune_n_reattach +
+                      params->prob_swap_nodes + params->prob_swap_subtrees;
+    const float pb = params->prob_beta_change / sum;
+    const float pp = params->prob_prune_n_reattach / sum;
+    const float ps = params->prob_swap_nodes / sum;
+    c->mp.cum_beta = pb;
+    c->mp.cum_prune = pb + pp;
+    c->mp.cum_swap = pb + pp + ps;
+    c->mp.beta_jump_sd = sd / params->beta_jump_scaling_chi;
+    c->q = pick_q((int)n_cells);
+    *out = c;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_create");
+  }
+}
+
+void bbs_destroy(bbs_ctx *c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_chains(c);
+  cudaFree(c->d_K);
+  cudaFree(c->d_M);
+  cudaFree(c->d_status);
+  if (c->h_cancel) cudaFreeHost(c->h_cancel);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int bbs_get_sizes(const bbs_ctx *c, uint32_t *n_cells, uint32_t *n_genes,
+                  uint32_t *n_chains) {
+  if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+  if (n_cells) *n_cells = c->n_cells;
+  if (n_genes) *n_genes = c->n_genes;
+  if (n_chains) *n_chains = c->n_chains;
+  return BBS_OK;
+}
+
+namespace {
+
+// Scores trees already on the device; optionally initialises chain states.
+int score_device(bbs_ctx *c, const uint32_t *d_rows, const float *betas,
+                 uint32_t n_trees, float *d_scores, uint64_t *d_counts,
+                 uint32_t *d_attach, ChainState *d_states) {
+  std::vector<float> terms(4 * (size_t)n_trees);
+  for (uint32_t t = 0; t < n_trees; t++) {
+    terms[4 * t] = betas[t];
+    host_beta_terms(c->ds, betas[t], &terms[4 * t + 1], &terms[4 * t + 2],
+                    &terms[4 * t + 3]);
+  }
+  DevBuf<float> d_terms;
+  BBS_CUDA(d_terms.alloc(terms.size()), "cudaMalloc");
+  BBS_CUDA(cudaMemcpyAsync(d_terms.p, terms.data(), sizeof(float) * terms.size(),
+                           cudaMemcpyHostToDevice, c->stream), "cudaMemcpy");
+  ScoreArgs a{};
+  a.ds = c->ds;
+  a.rows = d_rows;
+  a.beta_terms = d_terms.p;
+  a.n_trees = (int)n_trees;
+  a.scores = d_scores;
+  a.counts = d_counts;
+  a.attach = d_attach;
+  a.states = d_states;
+  const int e = launch_score(a, c->q, c->stream);
+  if (e != 0) return cuda_fail(e, "score kernel launch");
+  return sync_stream(c, "score kernel");
+}
+
+int upload_trees(bbs_ctx *c, const uint64_t *dm, uint32_t n_trees,
+                 uint32_t **d_out) {
+  const size_t words = (size_t)n_trees * c->n_nodes * c->W64;
+  cudaError_t e = cudaMalloc(d_out, sizeof(uint64_t) * std::max<size_t>(words, 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(*d_out, dm, sizeof(uint64_t) * words,
+                        cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_fail((int)e, "tree upload");
+  return BBS_OK;
+}
+
+}  // namespace
+
+int bbs_init_chains(bbs_ctx *c, uint32_t n_chains, const uint32_t *parents) {
+  try {
+    if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (n_chains < 1) return fail(BBS_ERR_INPUT, "need at least one chain");
+    const uint32_t n = c->n_nodes;
+    std::vector<uint32_t> pv((size_t)n_chains * n);
+    if (parents) {
+      for (uint32_t t = 0; t < n_chains; t++) {
+        const int r = check_parent_vector(parents + (size_t)t * n, n);
+        if (r != BBS_OK) return r;
+      }
+      std::memcpy(pv.data(), parents, sizeof(uint32_t) * pv.size());
+    } else {
+      random_parents(c->params.seed, c->n_genes, n_chains, pv.data());
+    }
+    const size_t tw = (size_t)n * c->W64;
+    std::vector<uint64_t> dm(tw * n_chains);
+    for (uint32_t t = 0; t < n_chains; t++)
+      parent_to_matrix(pv.data() + (size_t)t * n, n, nullptr, dm.data() + t * tw);
+    free_chains(c);
+    cudaError_t e = cudaMalloc(&c->d_rows, sizeof(uint64_t) * dm.size());
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_best, sizeof(uint64_t) * dm.size());
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_states, sizeof(ChainState) * n_chains);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(c->d_rows, dm.data(), sizeof(uint64_t) * dm.size(),
+                          cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(c->d_best, 0, sizeof(uint64_t) * dm.size(), c->stream);
+    if (e != cudaSuccess) {
+      free_chains(c);
+      return cuda_fail((int)e, "bbs_init_chains");
+    }
+    c->n_chains = n_chains;
+    std::vector<float> betas(n_chains, c->params.beta_mean);
+    const int r = score_device(c, c->d_rows, betas.data(), n_chains, nullptr,
+                               nullptr, nullptr, c->d_states);
+    if (r != BBS_OK) free_chains(c);
+    // Warps per block: one chain per warp, blocks spread evenly over SMs.
+    c->wpb = n_chains >= (uint32_t)c->n_sms * 16 ? 4 : 1;
+    return r;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_init_chains");
+  }
+}
+
+namespace {
+
+int start_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *d_moves,
+              bbs_step_trace *d_trace) {
+  RunArgs a{};
+  a.ds = c->ds;
+  a.mp = c->mp;
+  a.gamma = c->params.gamma;
+  a.n_chains = (int)c->n_chains;
+  a.n_steps = (int)n_steps;
+  a.seed = c->params.seed;
+  a.rows = c->d_rows;
+  a.best_rows = c->d_best;
+  a.states = c->d_states;
+  a.moves = d_moves;
+  a.trace = d_trace;
+  a.cancel = c->d_cancel;
+  a.status = c->d_status;
+  *c->h_cancel = 0;
+  BBS_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream), "cudaMemset");
+  BBS_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
+  const int e = launch_mcmc(a, c->q, c->wpb, c->n_sms, c->stream);
+  if (e != 0) return cuda_fail(e, "chain kernel launch");
+  BBS_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
+  return BBS_OK;
+}
+
+int finish_run(bbs_ctx *c) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  c->running = false;
+  if (e != cudaSuccess) return cuda_fail((int)e, "chain kernel");
+  e = cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+  if (e != cudaSuccess) return cuda_fail((int)e, "event timing");
+  int status = 0;
+  e = cudaMemcpy(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail((int)e, "status read");
+  if (status & 1) return fail(BBS_ERR_TIMEOUT, "the run was cancelled");
+  return BBS_OK;
+}
+
+}  // namespace
+
+int bbs_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *moves,
+            bbs_step_trace *trace) {
+  try {
+    if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (c->n_chains == 0) return fail(BBS_ERR_STATE, "bbs_init_chains was not called");
+    if (n_steps == 0) return BBS_OK;
+    if (n_steps > 0x7fffffffu) return fail(BBS_ERR_SIZE, "too many steps");
+    const size_t total = (size_t)c->n_chains * n_steps;
+    DevBuf<bbs_raw_move> d_moves;
+    DevBuf<bbs_step_trace> d_trace;
+    if (moves) {
+      for (size_t i = 0; i < total; i++) {
+        const bbs_raw_move &m = moves[i];
+        if (m.move_type < 0 || m.move_type > 3)
+          return fail(BBS_ERR_INPUT, "move %zu has type %d", i, m.move_type);
+        if (m.raw_v >= c->n_nodes || m.raw_w >= c->n_nodes)
+          return fail(BBS_ERR_INPUT, "move %zu names a node >= %u", i, c->n_nodes);
+      }
+      BBS_CUDA(d_moves.alloc(total), "cudaMalloc");
+      BBS_CUDA(cudaMemcpyAsync(d_moves.p, moves, sizeof(bbs_raw_move) * total,
+                               cudaMemcpyHostToDevice, c->stream), "cudaMemcpy");
+    }
+    if (trace) BBS_CUDA(d_trace.alloc(total), "cudaMalloc");
+    c->running = true;
+    int r = start_run(c, n_steps, d_moves.p, d_trace.p);
+    if (r != BBS_OK) {
+      c->running = false;
+      return r;
+    }
+    r = finish_run(c);
+    if (r == BBS_OK && trace)
+      BBS_CUDA(cudaMemcpy(trace, d_trace.p, sizeof(bbs_step_trace) * total,
+                          cudaMemcpyDeviceToHost), "trace copy");
+    return r;
+  } catch (...) {
+    c->running = false;
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_run");
+  }
+}
+
+int bbs_run_async(bbs_ctx *c, uint32_t n_steps) {
+  if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+  if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+  if (c->n_chains == 0) return fail(BBS_ERR_STATE, "bbs_init_chains was not called");
+  if (n_steps == 0) return BBS_OK;
+  c->running = true;
+  const int r = start_run(c, n_steps, nullptr, nullptr);
+  if (r != BBS_OK) c->running = false;
+  return r;
+}
+
+int bbs_sync(bbs_ctx *c) {
+  if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+  if (!c->running) return BBS_OK;
+  return finish_run(c);
+}
+
+int bbs_cancel(bbs_ctx *c) {
+  if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+  if (c->h_cancel) *(volatile int *)c->h_cancel = 1;
+  return BBS_OK;
+}
+
+int bbs_last_run_ms(const bbs_ctx *c, float *ms) {
+  if (!c || !ms) return fail(BBS_ERR_INPUT, "NULL argument");
+  *ms = c->last_ms;
+  return BBS_OK;
+}
+
+int bbs_get_best(bbs_ctx *c, uint64_t *am, uint64_t *dm, uint32_t *parent,
+                 float *beta, float *score, uint64_t *counts,
+                 uint32_t *chain) {
+  try {
+    if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (c->n_chains == 0) return fail(BBS_ERR_STATE, "no chains");
+    std::vector<ChainState> st(c->n_chains);
+    BBS_CUDA(cudaMemcpy(st.data(), c->d_states, sizeof(ChainState) * st.size(),
+                        cudaMemcpyDeviceToHost), "state copy");
+    // First chain in index order holding the maximum (the emulator's
+    // chain-major order, strict '>' as src/Application.hpp:456).
+    int best = -1;
+    for (uint32_t i = 0; i < c->n_chains; i++) {
+      if (!st[i].has_best) continue;
+      if (best < 0 || st[i].best_score > st[best].best_score) best = (int)i;
+    }
+    if (best < 0) return fail(BBS_ERR_STATE, "no steps have been run");
+    const uint32_t n = c->n_nodes;
+    const size_t tw = (size_t)n * c->W64;
+    std::vector<uint64_t> rows(tw);
+    BBS_CUDA(cudaMemcpy(rows.data(), c->d_best + (size_t)best * tw * 2,
+                        sizeof(uint64_t) * tw, cudaMemcpyDeviceToHost), "best copy");
+    if (dm) std::memcpy(dm, rows.data(), sizeof(uint64_t) * tw);
+    if (am) bbs_dm_to_am(rows.data(), n, am);
+    if (parent) matrix_to_parent(rows.data(), n, parent);
+    if (beta) *beta = st[best].best_beta;
+    if (score) *score = st[best].best_score;
+    if (counts) {
+      const int sk = st[best].best_sk, sm = st[best].best_sm;
+      counts[0] = (uint64_t)(c->ds.sum_k - c->ds.sum_m - sk + sm);
+      counts[1] = (uint64_t)(sk - sm);
+      counts[2] = (uint64_t)(c->ds.sum_m - sm);
+      counts[3] = (uint64_t)sm;
+    }
+    if (chain) *chain = (uint32_t)best;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_get_best");
+  }
+}
+
+int bbs_get_chains(bbs_ctx *c, uint64_t *dm, float *beta, float *score,
+                   uint64_t *counts) {
+  try {
+    if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (c->n_chains == 0) return fail(BBS_ERR_STATE, "no chains");
+    const size_t tw = (size_t)c->n_nodes * c->W64;
+    if (dm)
+      BBS_CUDA(cudaMemcpy(dm, c->d_rows, sizeof(uint64_t) * tw * c->n_chains,
+                          cudaMemcpyDeviceToHost), "row copy");
+    std::vector<ChainState> st(c->n_chains);
+    BBS_CUDA(cudaMemcpy(st.data(), c->d_states, sizeof(ChainState) * st.size(),
+                        cudaMemcpyDeviceToHost), "state copy");
+    for (uint32_t i = 0; i < c->n_chains; i++) {
+      if (beta) beta[i] = st[i].beta;
+      if (score) score[i] = st[i].score;
+      if (counts) {
+        const int sk = st[i].sk, sm = st[i].sm;
+        counts[4 * i + 0] = (uint64_t)(c->ds.sum_k - c->ds.sum_m - sk + sm);
+        counts[4 * i + 1] = (uint64_t)(sk - sm);
+        counts[4 * i + 2] = (uint64_t)(c->ds.sum_m - sm);
+        counts[4 * i + 3] = (uint64_t)sm;
+      }
+    }
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_get_chains");
+  }
+}
+
+int bbs_score_trees(bbs_ctx *c, const uint64_t *dm, const float *betas,
+                    uint32_t n_trees, float *scores, uint64_t *counts,
+                    uint32_t *attach) {
+  try {
+    if (!c || !dm || !betas || !scores) return fail(BBS_ERR_INPUT, "NULL argument");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (n_trees == 0) return BBS_OK;
+    for (uint32_t t = 0; t < n_trees; t++)
+      if (!(betas[t] > 0.0f && betas[t] < 1.0f))
+        return fail(BBS_ERR_INPUT, "beta of tree %u outside (0, 1)", t);
+    uint32_t *d_rows = nullptr;
+    int r = upload_trees(c, dm, n_trees, &d_rows);
+    if (r != BBS_OK) return r;
+    DevBuf<uint32_t> rows_guard;
+    rows_guard.p = d_rows;
+    DevBuf<float> d_scores;
+    DevBuf<uint64_t> d_counts;
+    DevBuf<uint32_t> d_attach;
+    BBS_CUDA(d_scores.alloc(n_trees), "cudaMalloc");
+    if (counts) BBS_CUDA(d_counts.alloc(4 * (size_t)n_trees), "cudaMalloc");
+    if (attach) BBS_CUDA(d_attach.alloc((size_t)n_trees * c->n_cells), "cudaMalloc");
+    r = score_device(c, d_rows, betas, n_trees, d_scores.p, d_counts.p,
+                     d_attach.p, nullptr);
+    if (r != BBS_OK) return r;
+    BBS_CUDA(cudaMemcpy(scores, d_scores.p, sizeof(float) * n_trees,
+                        cudaMemcpyDeviceToHost), "copy");
+    if (counts)
+      BBS_CUDA(cudaMemcpy(counts, d_counts.p, sizeof(uint64_t) * 4 * n_trees,
+                          cudaMemcpyDeviceToHost), "copy");
+    if (attach)
+      BBS_CUDA(cudaMemcpy(attach, d_attach.p,
+                          sizeof(uint32_t) * (size_t)n_trees * c->n_cells,
+                          cudaMemcpyDeviceToHost), "copy");
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_score_trees");
+  }
+}
+
+int bbs_apply_moves(bbs_ctx *c, const uint64_t *dm, const float *betas,
+                    uint32_t n_trees, const bbs_raw_move *raw,
+                    const bbs_move_params *params,
+                    bbs_move_params *params_out, uint64_t *dm_out,
+                    float *beta_out) {
+  try {
+    if (!c || !dm || !betas || !dm_out) return fail(BBS_ERR_INPUT, "NULL argument");
+    if (!raw && !params) return fail(BBS_ERR_INPUT, "need raw moves or move parameters");
+    if (n_trees == 0) return BBS_OK;
+    const uint32_t n = c->n_nodes;
+    for (uint32_t t = 0; t < n_trees; t++) {
+      const int type = raw ? raw[t].move_type : params[t].move_type;
+      if (type < 0 || type > 3) return fail(BBS_ERR_INPUT, "move %u has type %d", t, type);
+      if (raw && (raw[t].raw_v >= n || raw[t].raw_w >= n))
+        return fail(BBS_ERR_INPUT, "move %u names a node >= %u", t, n);
+      if (params) {
+        const bbs_move_params &p = params[t];
+        if (p.v >= n || p.w >= n || p.parent_of_v >= n || p.parent_of_w >= n ||
+            p.descendant_of_v >= n || p.nondescendant_of_v >= n)
+          return fail(BBS_ERR_INPUT, "move %u names a node >= %u", t, n);
+      }
+    }
+    uint32_t *d_rows = nullptr;
+    int r = upload_trees(c, dm, n_trees, &d_rows);
+    if (r != BBS_OK) return r;
+    DevBuf<uint32_t> rows_guard;
+    rows_guard.p = d_rows;
+    const size_t words = (size_t)n_trees * n * c->W64;
+    DevBuf<uint64_t> d_out;
+    DevBuf<float> d_betas, d_bout;
+    DevBuf<bbs_raw_move> d_raw;
+    DevBuf<bbs_move_params> d_par, d_pout;
+    BBS_CUDA(d_out.alloc(words), "cudaMalloc");
+    BBS_CUDA(d_betas.alloc(n_trees), "cudaMalloc");
+    BBS_CUDA(d_bout.alloc(n_trees), "cudaMalloc");
+    BBS_CUDA(d_pout.alloc(n_trees), "cudaMalloc");
+    BBS_CUDA(cudaMemcpyAsync(d_betas.p, betas, sizeof(float) * n_trees,
+                             cudaMemcpyHostToDevice, c->stream), "copy");
+    if (raw) {
+      BBS_CUDA(d_raw.alloc(n_trees), "cudaMalloc");
+      BBS_CUDA(cudaMemcpyAsync(d_raw.p, raw, sizeof(bbs_raw_move) * n_trees,
+                               cudaMemcpyHostToDevice, c->stream), "copy");
+    } else {
+      BBS_CUDA(d_par.alloc(n_trees), "cudaMalloc");
+      BBS_CUDA(cudaMemcpyAsync(d_par.p, params, sizeof(bbs_move_params) * n_trees,
+                               cudaMemcpyHostToDevice, c->stream), "copy");
+    }
+    BBS_CUDA(cudaMemsetAsync(d_out.p, 0, sizeof(uint64_t) * words, c->stream), "memset");
+    ApplyArgs a{};
+    a.n_nodes = (int)n;
+    a.n_trees = (int)n_trees;
+    a.rows = d_rows;
+    a.betas = d_betas.p;
+    a.raw = d_raw.p;
+    a.params = d_par.p;
+    a.params_out = d_pout.p;
+    a.rows_out = (uint32_t *)d_out.p;
+    a.beta_out = d_bout.p;
+    const int e = launch_apply(a, c->stream);
+    if (e != 0) return cuda_fail(e, "apply kernel launch");
+    r = sync_stream(c, "apply kernel");
+    if (r != BBS_OK) return r;
+    BBS_CUDA(cudaMemcpy(dm_out, d_out.p, sizeof(uint64_t) * words,
+                        cudaMemcpyDeviceToHost), "copy");
+    if (beta_out)
+      BBS_CUDA(cudaMemcpy(beta_out, d_bout.p, sizeof(float) * n_trees,
+                          cudaMemcpyDeviceToHost), "copy");
+    if (params_out)
+      BBS_CUDA(cudaMemcpy(params_out, d_pout.p, sizeof(bbs_move_params) * n_trees,
+                          cudaMemcpyDeviceToHost), "copy");
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_apply_moves");
+  }
+}
+
+int bbs_sumscore_grad(bbs_ctx *c, const uint64_t *dm, const float *alphas,
+                      const float *betas, uint32_t n_trees, float *logl,
+                      float *dalpha, float *dbeta, float *posterior) {
+  try {
+    if (!c || !dm || !alphas || !betas || !logl)
+      return fail(BBS_ERR_INPUT, "NULL argument");
+    if (n_trees == 0) return BBS_OK;
+    std::vector<float> tab(6 * (size_t)n_trees);
+    for (uint32_t t = 0; t < n_trees; t++) {
+      const double a = alphas[t], b = betas[t];
+      if (!(a > 0 && a < 1 && b > 0 && b < 1))
+        return fail(BBS_ERR_INPUT, "error rates of tree %u outside (0, 1)", t);
+      float *r = &tab[6 * t];
+      r[0] = alphas[t];
+      r[1] = betas[t];
+      r[2] = (float)std::log1p(-a);
+      r[3] = (float)std::log(b);
+      r[4] = (float)std::log(a);
+      r[5] = (float)std::log1p(-b);
+    }
+    uint32_t *d_rows = nullptr;
+    int r = upload_trees(c, dm, n_trees, &d_rows);
+    if (r != BBS_OK) return r;
+    DevBuf<uint32_t> rows_guard;
+    rows_guard.p = d_rows;
+    DevBuf<float> d_tab, d_out, d_post;
+    BBS_CUDA(d_tab.alloc(tab.size()), "cudaMalloc");
+    BBS_CUDA(d_out.alloc(3 * (size_t)n_trees), "cudaMalloc");
+    if (posterior)
+      BBS_CUDA(d_post.alloc((size_t)n_trees * c->n_cells * c->n_nodes), "cudaMalloc");
+    BBS_CUDA(cudaMemcpyAsync(d_tab.p, tab.data(), sizeof(float) * tab.size(),
+                             cudaMemcpyHostToDevice, c->stream), "copy");
+    GradArgs a{};
+    a.ds = c->ds;
+    a.rows = d_rows;
+    a.tables = d_tab.p;
+    a.n_trees = (int)n_trees;
+    a.logl = d_out.p;
+    a.dalpha = d_out.p + n_trees;
+    a.dbeta = d_out.p + 2 * (size_t)n_trees;
+    a.posterior = d_post.p;
+    const int e = launch_grad(a, c->q, c->stream);
+    if (e != 0) return cuda_fail(e, "adjoint kernel launch");
+    r = sync_stream(c, "adjoint kernel");
+    if (r != BBS_OK) return r;
+    std::vector<float> out(3 * (size_t)n_trees);
+    BBS_CUDA(cudaMemcpy(out.data(), d_out.p, sizeof(float) * out.size(),
+                        cudaMemcpyDeviceToHost), "copy");
+    std::memcpy(logl, out.data(), sizeof(float) * n_trees);
+    if (dalpha) std::memcpy(dalpha, out.data() + n_trees, sizeof(float) * n_trees);
+    if (dbeta) std::memcpy(dbeta, out.data() + 2 * n_trees, sizeof(float) * n_trees);
+    if (posterior)
+      BBS_CUDA(cudaMemcpy(posterior, d_post.p,
+                          sizeof(float) * (size_t)n_trees * c->n_cells * c->n_nodes,
+                          cudaMemcpyDeviceToHost), "copy");
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_sumscore_grad");
+  }
+}
+
+int bbs_popc_peak(double *popc_per_s, double *sm_clock_hz) {
+  if (!popc_per_s || !sm_clock_hz) return fail(BBS_ERR_INPUT, "NULL argument");
+  const int e = run_popc_bench(popc_per_s, sm_clock_hz);
+  if (e != 0) return cuda_fail(e, "popc benchmark");
+  return BBS_OK;
+}
+
+}  // extern "C"

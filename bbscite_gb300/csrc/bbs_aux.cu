@@ -1,0 +1,173 @@
+// bbs_aux.cu -- dispatch of the chain kernels, batch scorer / mover /
+// adjoint launchers and the integer-pipe calibration kernel.
+#include "bbs_launch.cuh"
+
+namespace bbs {
+
+int pick_q(int n_cells) {
+  // Keep every cell in registers when 32*Q covers the dataset; otherwise
+  // the widest chunk.
+  return std::min(kMaxQ, std::max(1, (n_cells + 31) / 32));
+}
+
+size_t mcmc_smem_bytes(int n_nodes, int wpb) {
+  const int rs = rs_of_w32(w32_of_nodes(n_nodes));
+  return (size_t)wpb * 2 * n_nodes * rs * sizeof(uint32_t);
+}
+
+int launch_mcmc(const RunArgs &a, int q, int wpb, int n_sms, void *stream) {
+  const int w32 = w32_of_nodes(a.ds.n_nodes);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (w32 > 4) q = std::min(q, 2);
+  if (w32 <= 4) return launch_mcmc_lo(a, w32, q, wpb, n_sms, s);
+  return launch_mcmc_hi(a, w32, q, wpb, n_sms, s);
+}
+
+template <int W32, bool ATTACH>
+static int launch_score_t(const ScoreArgs &a, cudaStream_t s) {
+  constexpr int RS = rs_of_w32(W32), WPB = 4, Q = 2;
+  const size_t smem = (size_t)WPB * a.ds.n_nodes * RS * sizeof(uint32_t);
+  cudaError_t e = prepare_smem(score_kernel<W32, Q, ATTACH>, smem);
+  if (e != cudaSuccess) return (int)e;
+  const int blocks = (a.n_trees + WPB - 1) / WPB;
+  score_kernel<W32, Q, ATTACH><<<blocks, WPB * 32, smem, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int launch_score(const ScoreArgs &a, int, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool att = a.attach != nullptr;
+  switch (w32_of_nodes(a.ds.n_nodes)) {
+#define BBS_SCORE_CASE(W) \
+  case W: return att ? launch_score_t<W, true>(a, s) : launch_score_t<W, false>(a, s);
+    BBS_SCORE_CASE(1)
+    BBS_SCORE_CASE(2)
+    BBS_SCORE_CASE(3)
+    BBS_SCORE_CASE(4)
+    BBS_SCORE_CASE(5)
+    BBS_SCORE_CASE(6)
+    BBS_SCORE_CASE(7)
+    BBS_SCORE_CASE(8)
+#undef BBS_SCORE_CASE
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+template <int W32>
+static int launch_apply_t(const ApplyArgs &a, cudaStream_t s) {
+  constexpr int RS = rs_of_w32(W32), WPB = 4;
+  const size_t smem = (size_t)WPB * a.n_nodes * RS * sizeof(uint32_t);
+  cudaError_t e = prepare_smem(apply_kernel<W32>, smem);
+  if (e != cudaSuccess) return (int)e;
+  apply_kernel<W32><<<(a.n_trees + WPB - 1) / WPB, WPB * 32, smem, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int launch_apply(const ApplyArgs &a, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (w32_of_nodes(a.n_nodes)) {
+    case 1: return launch_apply_t<1>(a, s);
+    case 2: return launch_apply_t<2>(a, s);
+    case 3: return launch_apply_t<3>(a, s);
+    case 4: return launch_apply_t<4>(a, s);
+    case 5: return launch_apply_t<5>(a, s);
+    case 6: return launch_apply_t<6>(a, s);
+    case 7: return launch_apply_t<7>(a, s);
+    case 8: return launch_apply_t<8>(a, s);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+template <int W32>
+static int launch_grad_t(const GradArgs &a, cudaStream_t s) {
+  constexpr int RS = rs_of_w32(W32), WPB = 4, Q = 2;
+  const size_t smem = (size_t)WPB * a.ds.n_nodes * RS * sizeof(uint32_t);
+  cudaError_t e = prepare_smem(grad_kernel<W32, Q>, smem);
+  if (e != cudaSuccess) return (int)e;
+  grad_kernel<W32, Q><<<(a.n_trees + WPB - 1) / WPB, WPB * 32, smem, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int launch_grad(const GradArgs &a, int, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (w32_of_nodes(a.ds.n_nodes)) {
+    case 1: return launch_grad_t<1>(a, s);
+    case 2: return launch_grad_t<2>(a, s);
+    case 3: return launch_grad_t<3>(a, s);
+    case 4: return launch_grad_t<4>(a, s);
+    case 5: return launch_grad_t<5>(a, s);
+    case 6: return launch_grad_t<6>(a, s);
+    case 7: return launch_grad_t<7>(a, s);
+    case 8: return launch_grad_t<8>(a, s);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Integer-pipe calibration: 8 independent popcounts per iteration per
+// thread (LOP3 + POPC + IADD each); the SM clock is read with clock64().
+// ------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) popc_bench_kernel(int iters,
+                                                         uint32_t *sink,
+                                                         long long *cycles) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t x[8], acc[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    x[i] = t * 2654435761u + 40503u * (uint32_t)i;
+    acc[i] = 0;
+  }
+  const long long t0 = clock64();
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) acc[i] += __popc(x[i] ^ (uint32_t)it);
+  }
+  const long long t1 = clock64();
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) s += acc[i];
+  if (s == 0xffffffffu) sink[t] = s;
+  if (threadIdx.x == 0 && blockIdx.x == 0) *cycles = t1 - t0;
+}
+
+int run_popc_bench(double *popc_per_s, double *clock_hz) {
+  int dev = 0, n_sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess)
+    e = cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return (int)e;
+  const int threads = 256, blocks = n_sms * 8, iters = 1 << 16;
+  uint32_t *sink = nullptr;
+  long long *cyc = nullptr;
+  e = cudaMalloc(&sink, sizeof(uint32_t) * threads * blocks);
+  if (e == cudaSuccess) e = cudaMalloc(&cyc, sizeof(long long));
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  float best_ms = 1e30f;
+  long long cycles = 0;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+    cudaEventRecord(a);
+    popc_bench_kernel<<<blocks, threads>>>(iters, sink, cyc);
+    cudaEventRecord(b);
+    e = cudaEventSynchronize(b);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    if (e == cudaSuccess && rep > 0 && ms < best_ms) {
+      best_ms = ms;
+      e = cudaMemcpy(&cycles, cyc, sizeof(long long), cudaMemcpyDeviceToHost);
+    }
+  }
+  if (e == cudaSuccess) {
+    const double ops = (double)threads * blocks * iters * 8.0;
+    *popc_per_s = ops / (best_ms * 1e-3);
+    *clock_hz = (double)cycles / (best_ms * 1e-3);
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFree(sink);
+  cudaFree(cyc);
+  return (int)e;
+}
+
+}  // namespace bbs

@@ -1,0 +1,533 @@
+// bbs_device.cuh -- warp-level building blocks of the chain step on sm_103a.
+//
+// One warp owns one chain.  The tree is kept only as its ancestor rows
+// (dm[x] = ancestors of x, src/MutationTree.hpp:718-723) in shared memory;
+// descendant sets are rebuilt on demand with one __ballot_sync per 32
+// nodes, so no transposed copy has to be updated.  Lane l owns nodes
+// x = 32 r + l (r < W32) for the update and cells c = 32 q + l for scoring.
+#pragma once
+#include <cstdint>
+
+#include "bbs_internal.h"
+
+namespace bbs {
+
+#define BBS_FULL_MASK 0xffffffffu
+
+// ------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) and the move sampler.  The word
+// assignment matches orc_sample_move in the CPU oracle.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += 0x9E3779B9u;
+    k.y += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__device__ __forceinline__ float u01_24(uint32_t x) {
+  return __uint2float_rn(x >> 8) * 5.9604644775390625e-08f;
+}
+
+__device__ __forceinline__ bbs_raw_move sample_move(const MoveProbs &mp,
+                                                    uint32_t n_nodes,
+                                                    uint64_t seed,
+                                                    uint32_t chain,
+                                                    uint64_t step) {
+  const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+  const uint4 a = philox4x32_10(
+      make_uint4((uint32_t)step, (uint32_t)(step >> 32), chain, 0u), key);
+  const uint4 b = philox4x32_10(
+      make_uint4((uint32_t)step, (uint32_t)(step >> 32), chain, 1u), key);
+  bbs_raw_move m;
+  const float ut = u01_24(a.x);
+  m.move_type = ut <= mp.cum_beta    ? BBS_MOVE_CHANGE_BETA
+                : ut <= mp.cum_prune ? BBS_MOVE_PRUNE_REATTACH
+                : ut <= mp.cum_swap  ? BBS_MOVE_SWAP_NODES
+                                     : BBS_MOVE_SWAP_SUBTREES;
+  uint32_t v = __umulhi(a.y, n_nodes - 1u);
+  uint32_t w = __umulhi(a.z, n_nodes - 2u);
+  if (w >= v) w++;
+  m.raw_v = v;
+  m.raw_w = w;
+  m.raw_descendant_of_v = u01_24(a.w);
+  m.raw_nondescendant_of_v = u01_24(b.x);
+  m.acceptance_level = u01_24(b.y);
+  const float u1 = (__uint2float_rn(b.z >> 8) + 1.0f) * 5.9604644775390625e-08f;
+  const float u2 = u01_24(b.w);
+  const float z = __fmul_rn(sqrtf(__fmul_rn(-2.0f, logf(u1))),
+                            cosf(__fmul_rn(6.2831853071795864769f, u2)));
+  m.beta_jump = __fmul_rn(z, mp.beta_jump_sd);
+  m.reserved = 0;
+  return m;
+}
+
+// ------------------------------------------------------------------------
+// Bit rows
+// ------------------------------------------------------------------------
+template <int W32>
+__device__ __forceinline__ void ld_row(const uint32_t *p, uint32_t (&a)[W32]) {
+  if constexpr (W32 == 1) {
+    a[0] = p[0];
+  } else if constexpr (W32 == 2) {
+    const uint2 t = *reinterpret_cast<const uint2 *>(p);
+    a[0] = t.x;
+    a[1] = t.y;
+  } else if constexpr (W32 <= 4) {
+    const uint4 t = *reinterpret_cast<const uint4 *>(p);
+    a[0] = t.x;
+    a[1] = t.y;
+    a[2] = t.z;
+    if constexpr (W32 == 4) a[3] = t.w;
+  } else if constexpr (W32 <= 6) {
+    const uint2 t0 = reinterpret_cast<const uint2 *>(p)[0];
+    const uint2 t1 = reinterpret_cast<const uint2 *>(p)[1];
+    const uint2 t2 = reinterpret_cast<const uint2 *>(p)[2];
+    a[0] = t0.x;
+    a[1] = t0.y;
+    a[2] = t1.x;
+    a[3] = t1.y;
+    a[4] = t2.x;
+    if constexpr (W32 == 6) a[5] = t2.y;
+  } else {
+    const uint4 t0 = reinterpret_cast<const uint4 *>(p)[0];
+    const uint4 t1 = reinterpret_cast<const uint4 *>(p)[1];
+    a[0] = t0.x;
+    a[1] = t0.y;
+    a[2] = t0.z;
+    a[3] = t0.w;
+    a[4] = t1.x;
+    a[5] = t1.y;
+    a[6] = t1.z;
+    if constexpr (W32 == 8) a[7] = t1.w;
+  }
+}
+
+// Stores all RS words of a row (padding words zero).
+template <int W32>
+__device__ __forceinline__ void st_row(uint32_t *p, const uint32_t (&a)[W32]) {
+  constexpr int RS = rs_of_w32(W32);
+  uint32_t t[RS];
+#pragma unroll
+  for (int k = 0; k < RS; k++) t[k] = k < W32 ? a[k] : 0u;
+  if constexpr (RS == 2) {
+    *reinterpret_cast<uint2 *>(p) = make_uint2(t[0], t[1]);
+  } else if constexpr (RS == 4) {
+    *reinterpret_cast<uint4 *>(p) = make_uint4(t[0], t[1], t[2], t[3]);
+  } else if constexpr (RS == 6) {
+    reinterpret_cast<uint2 *>(p)[0] = make_uint2(t[0], t[1]);
+    reinterpret_cast<uint2 *>(p)[1] = make_uint2(t[2], t[3]);
+    reinterpret_cast<uint2 *>(p)[2] = make_uint2(t[4], t[5]);
+  } else {
+    reinterpret_cast<uint4 *>(p)[0] = make_uint4(t[0], t[1], t[2], t[3]);
+    reinterpret_cast<uint4 *>(p)[1] = make_uint4(t[4], t[5], t[6], t[7]);
+  }
+}
+
+// a[idx] without dynamic register indexing.
+template <int W32>
+__device__ __forceinline__ uint32_t pick(const uint32_t (&a)[W32], uint32_t idx) {
+  uint32_t r = 0;
+#pragma unroll
+  for (int k = 0; k < W32; k++) r = (k == (int)idx) ? a[k] : r;
+  return r;
+}
+
+template <int W32>
+__device__ __forceinline__ uint32_t has_bit(const uint32_t (&a)[W32], uint32_t y) {
+  return (pick<W32>(a, y >> 5) >> (y & 31u)) & 1u;
+}
+
+// Bits of node group r (nodes 32r .. 32r+31) that exist in an n-node tree.
+__device__ __forceinline__ uint32_t group_mask(int r, int n) {
+  const int left = n - 32 * r;
+  return left >= 32 ? BBS_FULL_MASK : (left <= 0 ? 0u : ((1u << left) - 1u));
+}
+
+// k-th (0-based) set bit of a warp-uniform bit set S over W32 groups, or 0
+// if there is none (src/MutationTree.hpp:840-878).
+template <int W32>
+__device__ __forceinline__ uint32_t select_bit(const uint32_t (&S)[W32],
+                                               uint32_t k, int lane) {
+  uint32_t before = 0, result = 0;
+  bool found = false;
+#pragma unroll
+  for (int r = 0; r < W32; r++) {
+    const uint32_t c = __popc(S[r]);
+    if (!found && k < before + c) {  // warp-uniform branch
+      const uint32_t kk = k - before;
+      const bool hit = ((S[r] >> lane) & 1u) &&
+                       (uint32_t)__popc(S[r] & ((1u << lane) - 1u)) == kk;
+      const uint32_t b = __ballot_sync(BBS_FULL_MASK, hit);
+      result = 32u * r + (uint32_t)(__ffs(b) - 1);
+      found = true;
+    }
+    before += c;
+  }
+  return result;
+}
+
+// ------------------------------------------------------------------------
+// Move realisation and the proposed tree
+// ------------------------------------------------------------------------
+struct Realized {
+  bbs_move_params p;
+  int ndv, ndw;   // descendant counts of v and w (v, w included)
+  bool related;   // w is an ancestor of v
+};
+
+// Descendant sets of v and w as warp-uniform bit sets (one ballot per node
+// group: node x has v in its ancestor row <=> x is a descendant of v).
+template <int W32>
+__device__ __forceinline__ void descendant_sets(const uint32_t *rows, int n,
+                                                uint32_t v, uint32_t w,
+                                                int lane, uint32_t (&Dv)[W32],
+                                                uint32_t (&Dw)[W32]) {
+  constexpr int RS = rs_of_w32(W32);
+#pragma unroll
+  for (int r = 0; r < W32; r++) {
+    const int x = 32 * r + lane;
+    bool bv = false, bw = false;
+    if (x < n) {
+      const uint32_t *row = rows + x * RS;
+      bv = (row[v >> 5] >> (v & 31u)) & 1u;
+      bw = (row[w >> 5] >> (w & 31u)) & 1u;
+    }
+    Dv[r] = __ballot_sync(BBS_FULL_MASK, bv);
+    Dw[r] = __ballot_sync(BBS_FULL_MASK, bw);
+  }
+}
+
+// realize_raw_move_sample, src/MutationTree.hpp:323-363.  v, w must be
+// < n (the caller validates recorded moves; they are clamped here).
+template <int W32>
+__device__ __forceinline__ Realized realize_move(const uint32_t *rows, int n,
+                                                 float beta,
+                                                 const bbs_raw_move &raw,
+                                                 int lane, uint32_t (&Dv)[W32],
+                                                 uint32_t (&Dw)[W32]) {
+  constexpr int RS = rs_of_w32(W32);
+  Realized R;
+  uint32_t v = min(raw.raw_v, (uint32_t)(n - 1));
+  uint32_t w = min(raw.raw_w, (uint32_t)(n - 1));
+  // is_ancestor(v, w) <=> v is in w's ancestor row
+  if ((rows[w * RS + (v >> 5)] >> (v & 31u)) & 1u) {
+    const uint32_t t = v;
+    v = w;
+    w = t;
+  }
+  uint32_t Av[W32], Aw[W32];
+  ld_row<W32>(rows + v * RS, Av);
+  ld_row<W32>(rows + w * RS, Aw);
+  // Parents: the deepest proper ancestor (depth = ancestor count).
+  uint32_t kv = 0, kw = 0;
+#pragma unroll
+  for (int r = 0; r < W32; r++) {
+    const int x = 32 * r + lane;
+    bool bv = false, bw = false;
+    uint32_t depth = 0;
+    if (x < n) {
+      uint32_t a[W32];
+      ld_row<W32>(rows + x * RS, a);
+#pragma unroll
+      for (int k = 0; k < W32; k++) depth += __popc(a[k]);
+      bv = has_bit<W32>(a, v);
+      bw = has_bit<W32>(a, w);
+    }
+    Dv[r] = __ballot_sync(BBS_FULL_MASK, bv);
+    Dw[r] = __ballot_sync(BBS_FULL_MASK, bw);
+    const uint32_t key = (depth << 16) | (uint32_t)x;
+    if (x < n && ((Av[r] >> lane) & 1u) && (uint32_t)x != v) kv = max(kv, key);
+    if (x < n && ((Aw[r] >> lane) & 1u) && (uint32_t)x != w) kw = max(kw, key);
+  }
+  kv = __reduce_max_sync(BBS_FULL_MASK, kv);
+  kw = __reduce_max_sync(BBS_FULL_MASK, kw);
+  // A node without a proper ancestor is the root, its own parent.
+  R.p.parent_of_v = kv ? (kv & 0xffffu) : v;
+  R.p.parent_of_w = kw ? (kw & 0xffffu) : w;
+  int ndv = 0, ndw = 0;
+#pragma unroll
+  for (int r = 0; r < W32; r++) {
+    ndv += __popc(Dv[r]);
+    ndw += __popc(Dw[r]);
+  }
+  const int nnd = n - ndv;
+  const float fd = floorf(__fmul_rn(raw.raw_descendant_of_v, (float)ndv));
+  const float fn = floorf(__fmul_rn(raw.raw_nondescendant_of_v, (float)nnd));
+  const uint32_t i_desc = __float2uint_rz(fd);
+  const uint32_t i_nondesc = __float2uint_rz(fn);
+  uint32_t ND[W32];
+#pragma unroll
+  for (int r = 0; r < W32; r++) ND[r] = ~Dv[r] & group_mask(r, n);
+  R.p.move_type = raw.move_type;
+  R.p.v = v;
+  R.p.w = w;
+  R.p.descendant_of_v = select_bit<W32>(Dv, i_desc, lane);
+  R.p.nondescendant_of_v = select_bit<W32>(ND, i_nondesc, lane);
+  float nb = __fadd_rn(beta, raw.beta_jump);
+  if (nb < 0.0f) nb = fabsf(nb);
+  if (nb > 1.0f) nb = __fsub_rn(nb, __fmul_rn(2.0f, __fsub_rn(nb, 1.0f)));
+  R.p.new_beta = nb;
+  R.ndv = ndv;
+  R.ndw = ndw;
+  R.related = has_bit<W32>(Dw, v);
+  return R;
+}
+
+// The update constructor, src/MutationTree.hpp:123-307, on ancestor rows
+// only.  Lane l writes rows x = 32 r + l of `out`.  With D(x) the
+// descendant set and A(x) the ancestor row:
+//   SwapNodes(v,w):    A'(x) = swap_bits_vw(A(s(x))), s swaps v and w
+//   PruneReattach(v,t): x in D(v): A'(x) = A(t) | (A(x) & D(v))
+//   SwapSubtrees unrelated: x in D(v): A(pw) | (A(x) & D(v));
+//                           x in D(w): A(pv) | (A(x) & D(w))
+//   SwapSubtrees related (w above v, d = descendant_of_v):
+//                           x in D(v): A(x) & ~(D(w) & ~D(v));
+//                           x in D(w) \ D(v): A(x) | (A(d) & D(v))
+//   ChangeBeta: unchanged.
+// The same rules are checked bit-exactly against the reference's
+// per-bit rules by the tests.
+template <int W32>
+__device__ __forceinline__ void build_proposal(const uint32_t *rows,
+                                               uint32_t *out, int n,
+                                               const bbs_move_params &p,
+                                               const uint32_t (&Dv)[W32],
+                                               const uint32_t (&Dw)[W32],
+                                               bool related, int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  const uint32_t v = p.v, w = p.w;
+  uint32_t T1[W32], T2[W32];
+  const int type = p.move_type;
+  // Target rows (warp-uniform broadcast loads).
+  uint32_t t1 = 0, t2 = 0;
+  if (type == BBS_MOVE_PRUNE_REATTACH) {
+    t1 = p.nondescendant_of_v;
+  } else if (type == BBS_MOVE_SWAP_SUBTREES) {
+    t1 = p.parent_of_w;
+    t2 = related ? p.descendant_of_v : p.parent_of_v;
+  }
+  t1 = min(t1, (uint32_t)(n - 1));
+  t2 = min(t2, (uint32_t)(n - 1));
+  ld_row<W32>(rows + t1 * RS, T1);
+  ld_row<W32>(rows + t2 * RS, T2);
+#pragma unroll
+  for (int r = 0; r < W32; r++) {
+    const int x = 32 * r + lane;
+    if (x >= n) continue;
+    const bool in_v = (Dv[r] >> lane) & 1u;
+    const bool in_w = (Dw[r] >> lane) & 1u;
+    uint32_t a[W32];
+    if (type == BBS_MOVE_SWAP_NODES) {
+      const uint32_t src = (uint32_t)x == v ? w : ((uint32_t)x == w ? v : (uint32_t)x);
+      ld_row<W32>(rows + src * RS, a);
+      const uint32_t bv = has_bit<W32>(a, v), bw = has_bit<W32>(a, w);
+#pragma unroll
+      for (int k = 0; k < W32; k++) {
+        const uint32_t mv = (k == (int)(v >> 5)) ? (1u << (v & 31u)) : 0u;
+        const uint32_t mw = (k == (int)(w >> 5)) ? (1u << (w & 31u)) : 0u;
+        a[k] = (a[k] & ~(mv | mw)) | (bw ? mv : 0u) | (bv ? mw : 0u);
+      }
+    } else {
+      ld_row<W32>(rows + x * RS, a);
+      if (type == BBS_MOVE_PRUNE_REATTACH) {
+        if (in_v) {
+#pragma unroll
+          for (int k = 0; k < W32; k++) a[k] = T1[k] | (a[k] & Dv[k]);
+        }
+      } else if (type == BBS_MOVE_SWAP_SUBTREES) {
+        if (!related) {
+          if (in_v) {
+#pragma unroll
+            for (int k = 0; k < W32; k++) a[k] = T1[k] | (a[k] & Dv[k]);
+          } else if (in_w) {
+#pragma unroll
+            for (int k = 0; k < W32; k++) a[k] = T2[k] | (a[k] & Dw[k]);
+          }
+        } else {
+          if (in_v) {
+#pragma unroll
+            for (int k = 0; k < W32; k++) a[k] = a[k] & ~(Dw[k] & ~Dv[k]);
+          } else if (in_w) {
+#pragma unroll
+            for (int k = 0; k < W32; k++) a[k] = a[k] | (T2[k] & Dv[k]);
+          }
+        }
+      }
+    }
+    st_row<W32>(out + x * RS, a);
+  }
+}
+
+// ------------------------------------------------------------------------
+// Scoring (src/TreeScorer.hpp:131-210)
+// ------------------------------------------------------------------------
+// Exact int -> float for 0 <= n < 2^23 on the FP32/INT32 pipes.
+__device__ __forceinline__ float exact_float(int n) {
+  return __fsub_rn(__int_as_float(0x4B000000 + n), 8388608.0f);
+}
+
+// Per-(cell,node) score in the reference's order:
+// (((n00*l00 + n01*l01) + n10*l10) + n11*l11), no contraction.
+// From m = popc(M & A), k = popc(K & A): n11 = m, n01 = k - m,
+// n10 = popc(M) - m, n00 = popc(K) - popc(M) - k + m (M within K).
+__device__ __forceinline__ float pair_score(int k, int m, int pkm, int pm,
+                                            float l00, float l01, float l10,
+                                            float l11) {
+  const int n11 = m, n01 = k - m, n10 = pm - m, n00 = pkm - k + m;
+  float s = __fmul_rn(exact_float(n00), l00);
+  s = __fadd_rn(s, __fmul_rn(exact_float(n01), l01));
+  s = __fadd_rn(s, __fmul_rn(exact_float(n10), l10));
+  s = __fadd_rn(s, __fmul_rn(exact_float(n11), l11));
+  return s;
+}
+
+template <int W32, int Q>
+struct Cells {
+  uint32_t K[Q][W32], M[Q][W32];
+  int pkm[Q], pm[Q];
+};
+
+// Loads cells c = c0 + 32 q + lane (zero rows past n_cells: such a cell
+// has no counts and adds nothing).
+template <int W32, int Q>
+__device__ __forceinline__ void load_cells(Cells<W32, Q> &cb,
+                                           const DatasetDev &ds, int c0,
+                                           int lane) {
+  constexpr int RS = rs_of_w32(W32);
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int c = c0 + 32 * q + lane;
+    int pk = 0, pm = 0;
+#pragma unroll
+    for (int k = 0; k < W32; k++) {
+      uint32_t kw = 0, mw = 0;
+      if (c < ds.n_cells) {
+        kw = __ldg(ds.K + (size_t)c * RS + k);
+        mw = __ldg(ds.M + (size_t)c * RS + k);
+      }
+      cb.K[q][k] = kw;
+      cb.M[q][k] = mw;
+      pk += __popc(kw);
+      pm += __popc(mw);
+    }
+    cb.pkm[q] = pk - pm;
+    cb.pm[q] = pm;
+  }
+}
+
+// Max-over-attachments for the lane's Q cells against all n ancestor rows;
+// returns the lane's sums of k and m at the first-max node (ties keep the
+// lower node, std::max in src/TreeScorer.hpp:187-193).
+template <int W32, int Q, bool ATTACH>
+__device__ __forceinline__ void score_cells(const uint32_t *rows, int n,
+                                            const Cells<W32, Q> &cb, float l00,
+                                            float l01, float l10, float l11,
+                                            int &sk, int &sm, int (&att)[Q]) {
+  constexpr int RS = rs_of_w32(W32);
+  float best[Q];
+  uint32_t bkm[Q];
+  {
+    uint32_t a[W32];
+    ld_row<W32>(rows, a);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      int k = 0, m = 0;
+#pragma unroll
+      for (int w = 0; w < W32; w++) {
+        k += __popc(cb.K[q][w] & a[w]);
+        m += __popc(cb.M[q][w] & a[w]);
+      }
+      best[q] = pair_score(k, m, cb.pkm[q], cb.pm[q], l00, l01, l10, l11);
+      bkm[q] = (uint32_t)k | ((uint32_t)m << 16);
+      if constexpr (ATTACH) att[q] = 0;
+    }
+  }
+#pragma unroll 1
+  for (int j = 1; j < n; j++) {
+    uint32_t a[W32];
+    ld_row<W32>(rows + j * RS, a);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      int k = 0, m = 0;
+#pragma unroll
+      for (int w = 0; w < W32; w++) {
+        k += __popc(cb.K[q][w] & a[w]);
+        m += __popc(cb.M[q][w] & a[w]);
+      }
+      const float s = pair_score(k, m, cb.pkm[q], cb.pm[q], l00, l01, l10, l11);
+      const bool up = s > best[q];
+      best[q] = up ? s : best[q];
+      bkm[q] = up ? ((uint32_t)k | ((uint32_t)m << 16)) : bkm[q];
+      if constexpr (ATTACH) att[q] = up ? j : att[q];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    sk += (int)(bkm[q] & 0xffffu);
+    sm += (int)(bkm[q] >> 16);
+  }
+}
+
+// Whole-tree class sums (warp-reduced) over all cell chunks.
+template <int W32, int Q>
+__device__ __forceinline__ void score_tree(const uint32_t *rows, int n,
+                                           const DatasetDev &ds,
+                                           Cells<W32, Q> &cb, bool resident,
+                                           float l01, float l11, int lane,
+                                           int &sk, int &sm) {
+  int k = 0, m = 0, att[Q];
+  if (resident) {
+    score_cells<W32, Q, false>(rows, n, cb, ds.l00, l01, ds.l10, l11, k, m,
+                               att);
+  } else {
+    for (int c0 = 0; c0 < ds.n_cells; c0 += 32 * Q) {
+      load_cells<W32, Q>(cb, ds, c0, lane);
+      score_cells<W32, Q, false>(rows, n, cb, ds.l00, l01, ds.l10, l11, k, m,
+                                 att);
+    }
+  }
+  sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);
+  sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
+}
+
+// Class totals (n00, n01, n10, n11) from the sums.
+__device__ __forceinline__ void class_totals(const DatasetDev &ds, int sk,
+                                             int sm, int (&N)[4]) {
+  N[0] = ds.sum_k - ds.sum_m - sk + sm;
+  N[1] = sk - sm;
+  N[2] = ds.sum_m - sm;
+  N[3] = sm;
+}
+
+// ((l00*N00 + l01*N01) + l10*N10) + l11*N11 + prior, no contraction.
+__device__ __forceinline__ float tree_score(const DatasetDev &ds, int sk,
+                                           int sm, float l01, float l11,
+                                           float prior) {
+  int N[4];
+  class_totals(ds, sk, sm, N);
+  float t = __fmul_rn((float)N[0], ds.l00);
+  t = __fadd_rn(t, __fmul_rn((float)N[1], l01));
+  t = __fadd_rn(t, __fmul_rn((float)N[2], ds.l10));
+  t = __fadd_rn(t, __fmul_rn((float)N[3], l11));
+  return __fadd_rn(t, prior);
+}
+
+// The beta-dependent table entries (src/TreeScorer.hpp:136-137) and
+// logscore_beta (src/TreeScorer.hpp:122-126) for a new beta.
+__device__ __forceinline__ void beta_terms(const DatasetDev &ds, float beta,
+                                           float &l01, float &l11,
+                                           float &prior) {
+  l01 = logf(beta);
+  l11 = (float)log(1.0 - (double)beta);
+  float r = __fadd_rn(ds.lg_ab, __fmul_rn(__fsub_rn(ds.bpa, 1.0f), logf(beta)));
+  r = __fadd_rn(r, __fmul_rn(__fsub_rn(ds.bpb, 1.0f), logf(__fsub_rn(1.0f, beta))));
+  r = __fsub_rn(r, ds.lg_a);
+  prior = __fsub_rn(r, ds.lg_b);
+}
+
+}  // namespace bbs

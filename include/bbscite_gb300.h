@@ -1,0 +1,226 @@
+/*
+ * bbscite_gb300.h -- C ABI of the GB300 (sm_103a) implementation of
+ * bbSCITE's MCMC mutation-tree search.
+ *
+ * Plain C types only: caller-owned host buffers, sizes, an opaque context.
+ * No function throws or aborts; every entry point returns a BBS_* status and
+ * leaves a message for bbs_last_error().  One context is used by one host
+ * thread at a time; each context owns its device memory and one CUDA stream.
+ *
+ * Bit-row layout (identical to the reference's ac_int rows, little-endian):
+ *   n_nodes = n_genes + 1, root = n_nodes - 1, W = bbs_words(n_nodes)
+ *   uint64 words per row.  A tree is given by its ancestor rows
+ *   dm[x] (bit y <=> y is an ancestor of x, x itself and the root included)
+ *   and/or its descendant rows am[x] (bit y <=> x is an ancestor of y):
+ *   `descendant` / `ancestor` in src/MutationTree.hpp:40-71.
+ *   Cell data: per cell one row of W words, bit g = gene g:
+ *   `is_mutated` / `is_known` in src/main.cpp:103-144.
+ *
+ * References below are file:line in Janonard/bbSCITE.
+ */
+#ifndef BBSCITE_GB300_H
+#define BBSCITE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define BBS_API __attribute__((visibility("default")))
+#else
+#define BBS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference returns 1 from main / throws
+ * std::out_of_range: src/main.cpp:45-48, src/Parameters.hpp:465-467) ---- */
+#define BBS_OK 0
+#define BBS_ERR_INPUT 1   /* invalid argument or data */
+#define BBS_ERR_SIZE 2    /* size outside the supported range */
+#define BBS_ERR_CUDA 3    /* CUDA runtime error (no device, launch, ...) */
+#define BBS_ERR_TIMEOUT 4 /* a bounded run was cancelled / gave up */
+#define BBS_ERR_STATE 5   /* call order (e.g. run before init_chains) */
+#define BBS_ERR_IO 6      /* file could not be read or written */
+#define BBS_ERR_ALLOC 7   /* host or device allocation failed */
+
+#define BBS_MAX_GENES 255   /* replaces the compile-time 63/95 caps */
+#define BBS_MAX_CELLS 65535 /* integer class totals stay exact in FP32 */
+
+/* src/MoveType.hpp:23-42 */
+#define BBS_MOVE_CHANGE_BETA 0
+#define BBS_MOVE_PRUNE_REATTACH 1
+#define BBS_MOVE_SWAP_NODES 2
+#define BBS_MOVE_SWAP_SUBTREES 3
+
+/* Run parameters: the CLI surface of src/Parameters.hpp:39-45, 61-281.
+ * Move probabilities are normalised by their sum (Parameters.hpp:451-612). */
+typedef struct bbs_params {
+  float alpha_mean;            /* -fd  */
+  float beta_mean;             /* -ad  */
+  float beta_sd;               /* -sd  */
+  float prob_beta_change;      /* -e   */
+  float prob_prune_n_reattach; /* -move_probs a b c */
+  float prob_swap_nodes;
+  float prob_swap_subtrees;
+  float beta_jump_scaling_chi; /* -x   */
+  float gamma;                 /* -g   */
+  uint32_t reserved0;
+  uint64_t seed; /* Philox key for moves and random initial trees */
+} bbs_params;
+
+/* One recorded move, src/RawMoveDistribution.hpp:44-50 (32 bytes). */
+typedef struct bbs_raw_move {
+  int32_t move_type;
+  uint32_t raw_v, raw_w;
+  float raw_descendant_of_v, raw_nondescendant_of_v;
+  float beta_jump;
+  float acceptance_level;
+  uint32_t reserved;
+} bbs_raw_move;
+
+/* A realised move, src/MutationTree.hpp:84-89 (32 bytes). */
+typedef struct bbs_move_params {
+  int32_t move_type;
+  uint32_t v, w, parent_of_v, parent_of_w, descendant_of_v,
+      nondescendant_of_v;
+  float new_beta;
+} bbs_move_params;
+
+/* Per-step record written by bbs_run when a trace buffer is given. */
+typedef struct bbs_step_trace {
+  bbs_raw_move move;      /* the move as drawn (Philox) or read */
+  float proposed_score;   /* score of the proposal */
+  float current_score;    /* chain score after the step */
+  float proposed_beta;
+  uint32_t accepted;
+  uint64_t proposed_counts[4]; /* class totals n00,n01,n10,n11 */
+} bbs_step_trace;
+
+typedef struct bbs_ctx bbs_ctx;
+
+/* ---- library ---- */
+BBS_API const char *bbs_last_error(void);
+BBS_API const char *bbs_version(void);
+BBS_API uint32_t bbs_words(uint32_t n_nodes);
+/* Parameters() defaults, src/Parameters.hpp:39-45 */
+BBS_API void bbs_params_default(bbs_params *p);
+
+/* ---- host tree helpers (MutationTree host methods) ---- */
+/* src/MutationTree.hpp:427-476 */
+BBS_API int bbs_pruefer_to_parent_vector(const uint32_t *code, uint32_t code_len,
+                                 uint32_t *parent);
+/* src/MutationTree.hpp:379-409 */
+BBS_API int bbs_parent_vector_to_matrix(const uint32_t *parent, uint32_t n_nodes,
+                                uint64_t *am, uint64_t *dm);
+/* get_parent for every node, src/MutationTree.hpp:549-596 */
+BBS_API int bbs_matrix_to_parent_vector(const uint64_t *dm, uint32_t n_nodes,
+                                uint32_t *parent);
+/* descendant rows from ancestor rows (transpose) */
+BBS_API int bbs_dm_to_am(const uint64_t *dm, uint32_t n_nodes, uint64_t *am);
+/* to_graphviz / to_newick, src/MutationTree.hpp:799-837, 880-894.
+ * Writes at most cap bytes (NUL-terminated) and the full length. */
+BBS_API int bbs_tree_to_graphviz(const uint32_t *parent, uint32_t n_nodes, char *buf,
+                         size_t cap, size_t *len);
+BBS_API int bbs_tree_to_newick(const uint32_t *parent, uint32_t n_nodes, char *buf,
+                       size_t cap, size_t *len);
+/* Uniform random trees as in src/Application.hpp:149-157 (uniform Pruefer
+ * code, decoded), drawn from Philox(seed) instead of minstd_rand. */
+BBS_API int bbs_random_parent_vectors(uint64_t seed, uint32_t n_genes,
+                              uint32_t n_trees, uint32_t *parents);
+
+/* ---- input file (src/main.cpp:50-144) ----
+ * Parses a SCITE matrix (gene rows, cell columns, entries 0/1/2/3).  Call
+ * with mut == NULL to get the sizes; then with buffers of
+ * n_cells * bbs_words(n_genes + 1) words each. */
+BBS_API int bbs_read_csv(const char *path, uint32_t *n_cells, uint32_t *n_genes,
+                 uint64_t *is_mutated, uint64_t *is_known);
+
+/* ---- single-dataset context: Application + TreeScorer ---- */
+/* Application ctor data side + TreeScorer ctor (src/Application.hpp:88-117,
+ * src/TreeScorer.hpp:92-117): copies the cell bit rows to the device and
+ * builds the log table and the Beta prior. */
+BBS_API int bbs_create(bbs_ctx **ctx, const uint64_t *is_mutated,
+               const uint64_t *is_known, uint32_t n_cells, uint32_t n_genes,
+               const bbs_params *params);
+BBS_API void bbs_destroy(bbs_ctx *ctx);
+BBS_API int bbs_get_sizes(const bbs_ctx *ctx, uint32_t *n_cells, uint32_t *n_genes,
+                  uint32_t *n_chains);
+
+/* Initial chain states, src/Application.hpp:119-164: n_chains trees from
+ * `parents` (n_chains x n_nodes) or, when NULL, uniform random trees from
+ * the seed; beta = beta_mean; scores computed on the device.  Any chain
+ * count is accepted (the reference rounds up to the pipeline capacity,
+ * src/Application.hpp:105-117). */
+BBS_API int bbs_init_chains(bbs_ctx *ctx, uint32_t n_chains, const uint32_t *parents);
+
+/* The work kernel, src/Application.hpp:366-498: advances every chain by
+ * n_steps steps.  moves == NULL draws moves on the device from Philox
+ * (seed, chain, step); otherwise `moves` holds n_chains x n_steps recorded
+ * moves (chain-major, the emulator's order src/Application.hpp:313-354 with
+ * pipeline capacity 1).  `trace` (n_chains x n_steps, optional) receives
+ * every step.  Blocks until done.  The best proposal over all chains and
+ * all runs is kept (src/Application.hpp:456). */
+BBS_API int bbs_run(bbs_ctx *ctx, uint32_t n_steps, const bbs_raw_move *moves,
+            bbs_step_trace *trace);
+/* Same, returning immediately; bbs_sync waits and reports the status. */
+BBS_API int bbs_run_async(bbs_ctx *ctx, uint32_t n_steps);
+BBS_API int bbs_sync(bbs_ctx *ctx);
+/* Asks a running kernel to stop after its current step block; the run then
+ * returns BBS_ERR_TIMEOUT.  Safe from another host thread. */
+BBS_API int bbs_cancel(bbs_ctx *ctx);
+
+/* Device time in milliseconds of the last completed bbs_run / bbs_sync,
+ * measured with CUDA events recorded on the context's stream around the
+ * chain kernel (src/Application.hpp:197-219 reports the kernel makespan). */
+BBS_API int bbs_last_run_ms(const bbs_ctx *ctx, float *ms);
+
+/* get_best_am/dm/beta/score, src/Application.hpp:224-256; also the parent
+ * vector, the class totals (n00,n01,n10,n11) and the chain index.  Any
+ * output pointer may be NULL. */
+BBS_API int bbs_get_best(bbs_ctx *ctx, uint64_t *am, uint64_t *dm, uint32_t *parent,
+                 float *beta, float *score, uint64_t *counts,
+                 uint32_t *chain);
+/* Current chain states (dm rows n_chains x n_nodes x W, betas, scores). */
+BBS_API int bbs_get_chains(bbs_ctx *ctx, uint64_t *dm, float *beta, float *score,
+                   uint64_t *counts);
+
+/* TreeScorer::logscore_tree for a batch, src/TreeScorer.hpp:131-210:
+ * dm = n_trees x n_nodes x W ancestor rows, betas (n_trees).  Outputs:
+ * scores (class-total form: ((l00*N00 + l01*N01) + l10*N10) + l11*N11 plus
+ * logscore_beta), counts (n_trees x 4, may be NULL), attach (n_trees x
+ * n_cells first-max attachment nodes, may be NULL). */
+BBS_API int bbs_score_trees(bbs_ctx *ctx, const uint64_t *dm, const float *betas,
+                    uint32_t n_trees, float *scores, uint64_t *counts,
+                    uint32_t *attach);
+
+/* realize_raw_move_sample + update constructor for a batch,
+ * src/MutationTree.hpp:123-363.  When `raw` is non-NULL each move is
+ * realised first (params_out, optional, receives the result); otherwise
+ * `params` are applied as given.  dm_out receives the proposed ancestor
+ * rows, beta_out the proposed beta. */
+BBS_API int bbs_apply_moves(bbs_ctx *ctx, const uint64_t *dm, const float *betas,
+                    uint32_t n_trees, const bbs_raw_move *raw,
+                    const bbs_move_params *params,
+                    bbs_move_params *params_out, uint64_t *dm_out,
+                    float *beta_out);
+
+/* Sum-over-attachments score and its adjoint (no counterpart in the
+ * reference; SCITE's "-s" score, see docs/thesis/chapters/conclusion/
+ * open_directions.tex:13): logL = sum_c logsumexp_j s_cj(alpha, beta) and
+ * dlogL/dalpha, dlogL/dbeta for a batch of trees with per-tree (alpha,
+ * beta); posterior (n_trees x n_cells x n_nodes, optional) receives the
+ * attachment posteriors softmax_j s_cj.  No Beta prior term. */
+BBS_API int bbs_sumscore_grad(bbs_ctx *ctx, const uint64_t *dm, const float *alphas,
+                      const float *betas, uint32_t n_trees, float *logl,
+                      float *dalpha, float *dbeta, float *posterior);
+
+/* Integer-pipe calibration: 32-bit POPC throughput of this device in
+ * operations per second (a timed microbenchmark). */
+BBS_API int bbs_popc_peak(double *popc_per_s, double *sm_clock_hz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -404,7 +404,7 @@ float orc_logscore_tree(const orc_scorer *s0, const uint64_t *dm,
                         uint32_t *attach) {
   orc_scorer s = *s0;
   orc_scorer_set_beta(&s, beta);
-  const float L[2][2] = {{s.l00, s.l01}, {s.l10, s.l11}};
+  const float l00 = s.l00, l01 = s.l01, l10 = s.l10, l11 = s.l11;
   uint32_t W = orc_words(n_nodes);
   uint64_t tot[4] = {0, 0, 0, 0};
   float tree_score = 0.0f;
@@ -414,26 +414,28 @@ float orc_logscore_tree(const orc_scorer *s0, const uint64_t *dm,
     uint32_t best_j = 0, best_n[4] = {0, 0, 0, 0};
     for (uint32_t j = 0; j < n_nodes; j++) {
       const uint64_t *A = dm + (size_t)j * W;
-      uint32_t n[2][2];
-      float sc = 0.0f;
-      for (int o = 0; o < 2; o++) {
-        for (int t = 0; t < 2; t++) {
-          uint32_t cnt = 0;
-          for (uint32_t k = 0; k < W; k++) {
-            uint64_t occ = K[k] & (o ? M[k] : ~M[k]) & (t ? A[k] : ~A[k]);
-            cnt += (uint32_t)popc64(occ);
-          }
-          n[o][t] = cnt;
-          sc += (float)cnt * L[o][t];
-        }
+      /* popcount(known & (o ? mut : ~mut) & (t ? anc : ~anc)) */
+      uint32_t n00 = 0, n01 = 0, n10 = 0, n11 = 0;
+      for (uint32_t k = 0; k < W; k++) {
+        const uint64_t kn = K[k], mu = M[k], a = A[k];
+        n00 += (uint32_t)popc64(kn & ~mu & ~a);
+        n01 += (uint32_t)popc64(kn & ~mu & a);
+        n10 += (uint32_t)popc64(kn & mu & ~a);
+        n11 += (uint32_t)popc64(kn & mu & a);
       }
+      /* weighted in the order (0,0), (0,1), (1,0), (1,1) */
+      float sc = 0.0f;
+      sc += (float)n00 * l00;
+      sc += (float)n01 * l01;
+      sc += (float)n10 * l10;
+      sc += (float)n11 * l11;
       if (j == 0 || best < sc) {
         best = sc;
         best_j = j;
-        best_n[0] = n[0][0];
-        best_n[1] = n[0][1];
-        best_n[2] = n[1][0];
-        best_n[3] = n[1][1];
+        best_n[0] = n00;
+        best_n[1] = n01;
+        best_n[2] = n10;
+        best_n[3] = n11;
       }
     }
     tree_score += best;

@@ -51,10 +51,35 @@ class _MoveProbs(C.Structure):
                 ("cum_swap", C.c_float), ("beta_jump_sd", C.c_float)]
 
 
+def _foreign(path: str) -> bool:
+    """True when `path` exists but was built for another machine."""
+    import platform
+    want = {"x86_64": 0x3E, "aarch64": 0xB7}.get(platform.machine())
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    return (want is not None and len(head) == 20
+            and int.from_bytes(head[18:20], "little") != want)
+
+
 def build(ref: bool = True) -> None:
     """Builds liboracle.so (and _ref when the reference sources exist)."""
-    target = "all" if ref else "oracle"
-    subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+    import shutil
+    for path in (LIB_PATH, REF_PATH):
+        if _foreign(path):
+            os.unlink(path)
+    if shutil.which("make"):
+        target = "all" if ref else "oracle"
+        subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+        return
+    import platform
+    arch = ["-mpopcnt"] if platform.machine() == "x86_64" else []
+    subprocess.run(["gcc", "-O3", "-fPIC", "-ffp-contract=off", "-std=c11",
+                    *arch, "-shared", "-o", LIB_PATH,
+                    os.path.join(HERE, "bbs_oracle.c"), "-lm", "-lpthread"],
+                   check=True)
 
 
 _lib = None
@@ -68,7 +93,7 @@ def _p(a):
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        if not os.path.exists(LIB_PATH) or _foreign(LIB_PATH):
             build(ref=False)
         _lib = C.CDLL(LIB_PATH)
         v = C.c_void_p

@@ -31,3 +31,20 @@ def kat():
 def golden():
     import numpy as np
     return np.load(os.path.join(ROOT, "tests", "golden", "ref_vectors.npz"))
+
+
+@pytest.fixture(scope="session")
+def native():
+    """The in-tree native library (built on first use)."""
+    from bbscite_gb300 import build, native as N
+    build.build()
+    N.lib()
+    return N
+
+
+def has_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

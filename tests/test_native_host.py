@@ -1,0 +1,136 @@
+"""The native library on the host: it loads, exports every entry point that
+include/bbscite_gb300.h declares, and its host-side tree helpers and input
+parser reproduce the reference's known answers.  No GPU is needed."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from bbscite_gb300 import data as D
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "bbscite_gb300.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"BBS_API [^;]*?\b(bbs_\w+)\(", text)))
+
+
+def test_exports_every_declared_symbol(native):
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    L = C.CDLL(native.LIB_PATH)
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_defaults_match_reference_parameters(native):
+    p = native.default_params()
+    # src/Parameters.hpp:39-45
+    assert p.alpha_mean == pytest.approx(6.04e-5)
+    assert p.beta_mean == pytest.approx(0.4309)
+    assert p.beta_sd == pytest.approx(0.1)
+    assert (p.prob_beta_change, p.prob_prune_n_reattach, p.prob_swap_nodes,
+            p.prob_swap_subtrees) == pytest.approx((0.0, 0.55, 0.4, 0.05))
+    assert p.beta_jump_scaling_chi == 10.0 and p.gamma == 1.0
+
+
+def test_host_tree_helpers_kat(native, kat):
+    k = kat["pruefer_code_to_parent_vector"]
+    assert native.pruefer_to_parent(k["code"]).tolist() == k["expected"]
+    k = kat["parent_vector_to_matrix"]
+    am, dm = native.parent_to_matrix(k["parent_vector"])
+    assert [int(r[0]) for r in am] == [int(s, 2) for s in k["am"]]
+    assert [int(r[0]) for r in dm] == [int(s, 2) for s in k["dm"]]
+    assert (native.dm_to_am(dm) == am).all()
+    assert native.matrix_to_parent(dm).tolist() == k["parent_vector"]
+    pv = kat["to_graphviz"]["parent_vector"]
+    assert native.to_graphviz(pv) == kat["to_graphviz"]["expected"]
+    assert native.to_newick(pv) == kat["to_newick"]["expected"]
+
+
+def test_host_helpers_match_oracle(native, orc):
+    rng = np.random.default_rng(5)
+    for G in (2, 5, 31, 63, 64, 95, 127, 128, 200, 255):
+        code = rng.integers(0, G + 1, size=G - 1)
+        pv = native.pruefer_to_parent(code)
+        assert (pv == orc.pruefer_to_parent(code)).all()
+        am, dm = native.parent_to_matrix(pv)
+        oam, odm = orc.parent_to_matrix(pv)
+        assert (am == oam).all() and (dm == odm).all()
+        assert (native.matrix_to_parent(dm) == orc.parent_vector(dm)).all()
+
+
+def test_random_parents_are_valid_trees(native):
+    P = native.random_parents(123, 95, 64)
+    assert P.shape == (64, 96)
+    for pv in P:
+        native.parent_to_matrix(pv)  # raises on an invalid tree
+    assert not (P[0] == P[1]).all()
+    assert (native.random_parents(123, 95, 64) == P).all()
+
+
+def test_invalid_parent_vectors_are_rejected(native):
+    with pytest.raises(native.BbsError) as e:
+        native.parent_to_matrix([1, 0, 3, 3])  # cycle 0 -> 1 -> 0
+    assert e.value.code == native.BBS_ERR_INPUT
+    with pytest.raises(native.BbsError):
+        native.parent_to_matrix([3, 0, 1, 2])  # root not its own parent
+    with pytest.raises(native.BbsError):
+        native.parent_to_matrix([9, 3, 3, 3])  # out of range
+
+
+def test_read_csv_matches_generator(native, tmp_path):
+    m, _, _ = D.generate_dataset(3, 40, 70, 1e-2, 0.2, 0.1, 0.05)
+    path = str(tmp_path / "in.csv")
+    D.write_csv(m, path)
+    mut, known, nc, ng = native.read_csv(path)
+    assert (nc, ng) == (70, 40)
+    em, ek = D.matrix_to_bits(m)
+    assert (mut == em).all() and (known == ek).all()
+
+
+@pytest.mark.parametrize("text,err", [
+    ("0 1 2\n0 1\n", "Inconsistent rows"),
+    ("0 1 x\n", "Illegal character"),
+    ("", "Empty input file"),
+])
+def test_read_csv_errors(native, tmp_path, text, err):
+    path = tmp_path / "bad.csv"
+    path.write_text(text)
+    with pytest.raises(native.BbsError) as e:
+        native.read_csv(str(path))
+    assert err in str(e.value)
+
+
+def test_read_csv_size_cap(native, tmp_path):
+    path = tmp_path / "wide.csv"
+    path.write_text("\n".join(["0 1"] * 256) + "\n")
+    with pytest.raises(native.BbsError) as e:
+        native.read_csv(str(path))
+    assert e.value.code == native.BBS_ERR_SIZE
+
+
+def test_create_without_gpu_fails_cleanly(native):
+    from conftest import has_gpu
+    if has_gpu():
+        pytest.skip("a GPU is present")
+    mut = np.zeros((4, 1), dtype=np.uint64)
+    with pytest.raises(native.BbsError) as e:
+        native.Context(mut, mut, 4, 10)
+    assert e.value.code == native.BBS_ERR_CUDA
+
+
+def test_create_validates_arguments(native):
+    mut = np.zeros((4, 1), dtype=np.uint64)
+    with pytest.raises(native.BbsError) as e:
+        native.Context(mut, mut, 4, 1)  # fewer than 2 genes
+    assert e.value.code == native.BBS_ERR_SIZE
+    p = native.default_params(prob_beta_change=0.0, prob_prune_n_reattach=0.0,
+                              prob_swap_nodes=0.0, prob_swap_subtrees=0.0)
+    with pytest.raises(native.BbsError) as e:
+        native.Context(mut, mut, 4, 10, p)
+    assert "sum of the move type probabilities is zero" in str(e.value)
