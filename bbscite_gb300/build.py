@@ -26,7 +26,10 @@ LIB = os.path.join(PKG, "libbbscite_gb300.so")
 CLI = os.path.join(PKG, "bin", "bbscite")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code rounds every float operation as written (no FMA contraction),
+# like the reference's scorer constants and the oracle.
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-ffp-contract=off",
               "-Xcompiler", "-fvisibility=hidden", "-I" + INCLUDE,
               "-I" + CSRC]
 UNITS = ["bbs_mcmc_lo.cu", "bbs_mcmc_hi.cu", "bbs_aux.cu", "bbs_api.cu",
@@ -98,7 +101,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             max(os.path.getmtime(LIB), os.path.getmtime(cli_src),
                 _deps())):
         r = subprocess.run(
-            ["g++", "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC,
+            ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC,
              cli_src, "-o", CLI, "-L" + PKG, "-lbbscite_gb300",
              "-Wl,-rpath,$ORIGIN/.."], capture_output=True, text=True)
         if r.returncode != 0:

@@ -107,9 +107,15 @@ int launch_grad(const GradArgs &a, int, void *stream) {
 // Integer-pipe calibration: 8 independent popcounts per iteration per
 // thread (LOP3 + POPC + IADD each); the SM clock is read with clock64().
 // ------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 __global__ void __launch_bounds__(256) popc_bench_kernel(int iters,
                                                          uint32_t *sink,
-                                                         long long *cycles) {
+                                                         long long *clock_probe) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t x[8], acc[8];
 #pragma unroll
@@ -117,17 +123,22 @@ __global__ void __launch_bounds__(256) popc_bench_kernel(int iters,
     x[i] = t * 2654435761u + 40503u * (uint32_t)i;
     acc[i] = 0;
   }
-  const long long t0 = clock64();
+  const long long c0 = clock64();
+  const uint64_t g0 = global_ns();
   for (int it = 0; it < iters; it++) {
 #pragma unroll
     for (int i = 0; i < 8; i++) acc[i] += __popc(x[i] ^ (uint32_t)it);
   }
-  const long long t1 = clock64();
+  const long long c1 = clock64();
+  const uint64_t g1 = global_ns();
   uint32_t s = 0;
 #pragma unroll
   for (int i = 0; i < 8; i++) s += acc[i];
   if (s == 0xffffffffu) sink[t] = s;
-  if (threadIdx.x == 0 && blockIdx.x == 0) *cycles = t1 - t0;
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    clock_probe[0] = c1 - c0;
+    clock_probe[1] = (long long)(g1 - g0);
+  }
 }
 
 int run_popc_bench(double *popc_per_s, double *clock_hz) {
@@ -140,12 +151,12 @@ int run_popc_bench(double *popc_per_s, double *clock_hz) {
   uint32_t *sink = nullptr;
   long long *cyc = nullptr;
   e = cudaMalloc(&sink, sizeof(uint32_t) * threads * blocks);
-  if (e == cudaSuccess) e = cudaMalloc(&cyc, sizeof(long long));
+  if (e == cudaSuccess) e = cudaMalloc(&cyc, 2 * sizeof(long long));
   cudaEvent_t a = nullptr, b = nullptr;
   if (e == cudaSuccess) e = cudaEventCreate(&a);
   if (e == cudaSuccess) e = cudaEventCreate(&b);
   float best_ms = 1e30f;
-  long long cycles = 0;
+  long long probe[2] = {0, 1};
   for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
     cudaEventRecord(a);
     popc_bench_kernel<<<blocks, threads>>>(iters, sink, cyc);
@@ -155,13 +166,14 @@ int run_popc_bench(double *popc_per_s, double *clock_hz) {
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
     if (e == cudaSuccess && rep > 0 && ms < best_ms) {
       best_ms = ms;
-      e = cudaMemcpy(&cycles, cyc, sizeof(long long), cudaMemcpyDeviceToHost);
+      e = cudaMemcpy(probe, cyc, 2 * sizeof(long long), cudaMemcpyDeviceToHost);
     }
   }
   if (e == cudaSuccess) {
     const double ops = (double)threads * blocks * iters * 8.0;
     *popc_per_s = ops / (best_ms * 1e-3);
-    *clock_hz = (double)cycles / (best_ms * 1e-3);
+    // SM cycles over global-timer nanoseconds of one block
+    *clock_hz = (double)probe[0] / ((double)probe[1] * 1e-9);
   }
   if (a) cudaEventDestroy(a);
   if (b) cudaEventDestroy(b);

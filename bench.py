@@ -227,7 +227,7 @@ def _traffic_from_profile():
         return None
     with open(p) as f:
         d = json.load(f)
-    return d.get("dram_bytes_per_chain_step")
+    return d.get("dram_bytes_per_chain_per_launch")
 
 
 def run_ours(args) -> None:
@@ -329,7 +329,9 @@ def run_ours(args) -> None:
             "bound": "int (POPC pipe)", "achieved": achieved / 1e9,
             "peak": peak / 1e9, "unit": "Gop/s",
             "frac": achieved / peak,
-            "traffic": (traffic * chains * L) if traffic is not None else None,
+            "traffic": (traffic * chains) if traffic is not None else None,
+            "traffic_unit": "bytes per launch (ncu dram read+write, "
+                            "profiles/mcmc_95x96_dram.json)",
             "peak_source": "bbs_popc_peak microbenchmark on this GPU "
                            f"(SM clock {clk_hz / 1e6:.0f} MHz)",
             "work_per_chain_step": f"{popc_step} POPC (32-bit)",
