@@ -224,7 +224,7 @@ struct bbs_ctx {
   int *d_status = nullptr;
   int *h_cancel = nullptr;        // mapped pinned flag
   int *d_cancel = nullptr;
-  int q = 1, wpb = 1;
+  int q = 1, wpc = 1, cpb = 1;  // chain-kernel launch shape
   bool running = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.0f;
@@ -600,6 +600,33 @@ int score_device(bbs_ctx *c, const uint32_t *d_rows, const float *betas,
   return sync_stream(c, "score kernel");
 }
 
+// Launch shape without timing: split the cells over up to four warps per
+// chain when there are too few chains to give every scheduler ~3 warps,
+// preferring shapes that leave no cell slots empty.
+void default_launch(bbs_ctx *c) {
+  const int groups = (int)((c->n_cells + 31) / 32);
+  const int qmax = w32_of_nodes((int)c->n_nodes) > 4 ? 2 : kMaxQ;
+  double best = 1e30;
+  for (int wpc = 1; wpc <= 4; wpc++) {
+    const int q = std::max(1, (groups + wpc - 1) / wpc);
+    if (q > qmax) continue;
+    const double waste = (double)(wpc * q) / groups;
+    const double warps = (double)c->n_chains * wpc;
+    const double occ = std::min(1.0, warps / (12.0 * c->n_sms));
+    const double est = waste / occ * (1.0 + 0.1 * (wpc - 1));
+    if (est < best) {
+      best = est;
+      c->wpc = wpc;
+      c->q = q;
+    }
+  }
+  if (best >= 1e30) {  // very wide datasets: chunks of qmax per lane
+    c->wpc = 4;
+    c->q = qmax;
+  }
+  c->cpb = c->wpc == 1 ? (c->n_chains >= (uint32_t)c->n_sms * 16 ? 4 : 1) : 1;
+}
+
 int upload_trees(bbs_ctx *c, const uint64_t *dm, uint32_t n_trees,
                  uint32_t **d_out) {
   const size_t words = (size_t)n_trees * c->n_nodes * c->W64;
@@ -651,8 +678,7 @@ int bbs_init_chains(bbs_ctx *c, uint32_t n_chains, const uint32_t *parents) {
     const int r = score_device(c, c->d_rows, betas.data(), n_chains, nullptr,
                                nullptr, nullptr, c->d_states);
     if (r != BBS_OK) free_chains(c);
-    // Warps per block: one chain per warp, blocks spread evenly over SMs.
-    c->wpb = n_chains >= (uint32_t)c->n_sms * 16 ? 4 : 1;
+    default_launch(c);
     return r;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_init_chains");
@@ -677,10 +703,11 @@ int start_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *d_moves,
   a.trace = d_trace;
   a.cancel = c->d_cancel;
   a.status = c->d_status;
+  a.wpc = c->wpc;
   *c->h_cancel = 0;
   BBS_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream), "cudaMemset");
   BBS_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
-  const int e = launch_mcmc(a, c->q, c->wpb, c->n_sms, c->stream);
+  const int e = launch_mcmc(a, c->q, c->cpb, c->n_sms, c->stream);
   if (e != 0) return cuda_fail(e, "chain kernel launch");
   BBS_CUDA(cudaEventRecord(c->ev1, c->stream), "cudaEventRecord");
   return BBS_OK;
@@ -763,6 +790,91 @@ int bbs_cancel(bbs_ctx *c) {
   if (!c) return fail(BBS_ERR_INPUT, "NULL context");
   if (c->h_cancel) *(volatile int *)c->h_cancel = 1;
   return BBS_OK;
+}
+
+int bbs_set_launch(bbs_ctx *c, int cells_per_lane, int warps_per_chain,
+                   int chains_per_block) {
+  if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+  const int qmax = w32_of_nodes((int)c->n_nodes) > 4 ? 2 : kMaxQ;
+  if (cells_per_lane < 0 || cells_per_lane > qmax)
+    return fail(BBS_ERR_INPUT, "cells per lane must be in [1, %d]", qmax);
+  if (warps_per_chain < 0 || warps_per_chain > 4)
+    return fail(BBS_ERR_INPUT, "warps per chain must be in [1, 4]");
+  if (chains_per_block < 0 || chains_per_block > 4)
+    return fail(BBS_ERR_INPUT, "chains per block must be in [1, 4]");
+  if (cells_per_lane) c->q = cells_per_lane;
+  if (warps_per_chain) c->wpc = warps_per_chain;
+  if (chains_per_block) c->cpb = chains_per_block;
+  if (c->wpc > 1) c->cpb = 1;
+  return BBS_OK;
+}
+
+int bbs_get_launch(const bbs_ctx *c, int *cells_per_lane,
+                   int *warps_per_chain, int *chains_per_block) {
+  if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+  if (cells_per_lane) *cells_per_lane = c->q;
+  if (warps_per_chain) *warps_per_chain = c->wpc;
+  if (chains_per_block) *chains_per_block = c->cpb;
+  return BBS_OK;
+}
+
+int bbs_autotune(bbs_ctx *c, uint32_t probe_steps, float *best_ms) {
+  try {
+    if (!c) return fail(BBS_ERR_INPUT, "NULL context");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (c->n_chains == 0) return fail(BBS_ERR_STATE, "bbs_init_chains was not called");
+    if (probe_steps == 0) probe_steps = 64;
+    // Keep the chains as they are: save, probe, restore.
+    const size_t rows_bytes = sizeof(uint64_t) * c->n_chains * c->n_nodes * c->W64;
+    DevBuf<uint8_t> save_rows, save_best, save_states;
+    BBS_CUDA(save_rows.alloc(rows_bytes), "cudaMalloc");
+    BBS_CUDA(save_best.alloc(rows_bytes), "cudaMalloc");
+    BBS_CUDA(save_states.alloc(sizeof(ChainState) * c->n_chains), "cudaMalloc");
+    auto copy = [&](void *dst, const void *src, size_t b) {
+      return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, c->stream);
+    };
+    BBS_CUDA(copy(save_rows.p, c->d_rows, rows_bytes), "save");
+    BBS_CUDA(copy(save_best.p, c->d_best, rows_bytes), "save");
+    BBS_CUDA(copy(save_states.p, c->d_states, sizeof(ChainState) * c->n_chains), "save");
+    const int groups = (int)((c->n_cells + 31) / 32);
+    const int qmax = w32_of_nodes((int)c->n_nodes) > 4 ? 2 : kMaxQ;
+    const int q0 = c->q, w0 = c->wpc, b0 = c->cpb;
+    float best = 1e30f;
+    int bq = q0, bw = w0, bb = b0;
+    for (int wpc = 1; wpc <= 4; wpc++)
+      for (int q = 1; q <= qmax; q++) {
+        if (wpc * q > groups + 1) continue;  // mostly empty cell slots
+        for (int cpb : {1, 2, 4}) {
+          if (wpc > 1 && cpb > 1) continue;
+          c->q = q;
+          c->wpc = wpc;
+          c->cpb = cpb;
+          c->running = true;
+          int r = start_run(c, probe_steps, nullptr, nullptr);
+          if (r == BBS_OK) r = finish_run(c);
+          c->running = false;
+          if (r == BBS_OK && c->last_ms < best) {
+            best = c->last_ms;
+            bq = q;
+            bw = wpc;
+            bb = cpb;
+          }
+          BBS_CUDA(copy(c->d_rows, save_rows.p, rows_bytes), "restore");
+          BBS_CUDA(copy(c->d_best, save_best.p, rows_bytes), "restore");
+          BBS_CUDA(copy(c->d_states, save_states.p,
+                        sizeof(ChainState) * c->n_chains), "restore");
+        }
+      }
+    c->q = bq;
+    c->wpc = bw;
+    c->cpb = bb;
+    const int r = sync_stream(c, "autotune restore");
+    if (best_ms) *best_ms = best;
+    return r;
+  } catch (...) {
+    c->running = false;
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_autotune");
+  }
 }
 
 int bbs_last_run_ms(const bbs_ctx *c, float *ms) {

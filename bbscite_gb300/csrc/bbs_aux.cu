@@ -10,17 +10,17 @@ int pick_q(int n_cells) {
   return std::min(kMaxQ, std::max(1, (n_cells + 31) / 32));
 }
 
-size_t mcmc_smem_bytes(int n_nodes, int wpb) {
+size_t mcmc_smem_bytes(int n_nodes, int wpc, int cpb) {
   const int rs = rs_of_w32(w32_of_nodes(n_nodes));
-  return (size_t)wpb * 2 * n_nodes * rs * sizeof(uint32_t);
+  return (size_t)cpb * slot_words(n_nodes, rs, wpc) * sizeof(uint32_t);
 }
 
-int launch_mcmc(const RunArgs &a, int q, int wpb, int n_sms, void *stream) {
+int launch_mcmc(const RunArgs &a, int q, int cpb, int n_sms, void *stream) {
   const int w32 = w32_of_nodes(a.ds.n_nodes);
   cudaStream_t s = (cudaStream_t)stream;
   if (w32 > 4) q = std::min(q, 2);
-  if (w32 <= 4) return launch_mcmc_lo(a, w32, q, wpb, n_sms, s);
-  return launch_mcmc_hi(a, w32, q, wpb, n_sms, s);
+  if (w32 <= 4) return launch_mcmc_lo(a, w32, q, cpb, n_sms, s);
+  return launch_mcmc_hi(a, w32, q, cpb, n_sms, s);
 }
 
 template <int W32, bool ATTACH>

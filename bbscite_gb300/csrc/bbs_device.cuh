@@ -34,11 +34,13 @@ __device__ __forceinline__ float u01_24(uint32_t x) {
   return __uint2float_rn(x >> 8) * 5.9604644775390625e-08f;
 }
 
+// The normal jump is only drawn when it is used (beta moves) or recorded.
 __device__ __forceinline__ bbs_raw_move sample_move(const MoveProbs &mp,
                                                     uint32_t n_nodes,
                                                     uint64_t seed,
                                                     uint32_t chain,
-                                                    uint64_t step) {
+                                                    uint64_t step,
+                                                    bool always_jump) {
   const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
   const uint4 a = philox4x32_10(
       make_uint4((uint32_t)step, (uint32_t)(step >> 32), chain, 0u), key);
@@ -58,11 +60,15 @@ __device__ __forceinline__ bbs_raw_move sample_move(const MoveProbs &mp,
   m.raw_descendant_of_v = u01_24(a.w);
   m.raw_nondescendant_of_v = u01_24(b.x);
   m.acceptance_level = u01_24(b.y);
-  const float u1 = (__uint2float_rn(b.z >> 8) + 1.0f) * 5.9604644775390625e-08f;
-  const float u2 = u01_24(b.w);
-  const float z = __fmul_rn(sqrtf(__fmul_rn(-2.0f, logf(u1))),
-                            cosf(__fmul_rn(6.2831853071795864769f, u2)));
-  m.beta_jump = __fmul_rn(z, mp.beta_jump_sd);
+  m.beta_jump = 0.0f;
+  if (always_jump || m.move_type == BBS_MOVE_CHANGE_BETA) {
+    const float u1 =
+        (__uint2float_rn(b.z >> 8) + 1.0f) * 5.9604644775390625e-08f;
+    const float u2 = u01_24(b.w);
+    const float z = __fmul_rn(sqrtf(__fmul_rn(-2.0f, logf(u1))),
+                              cosf(__fmul_rn(6.2831853071795864769f, u2)));
+    m.beta_jump = __fmul_rn(z, mp.beta_jump_sd);
+  }
   m.reserved = 0;
   return m;
 }
@@ -292,13 +298,15 @@ __device__ __forceinline__ Realized realize_move(const uint32_t *rows, int n,
 //   ChangeBeta: unchanged.
 // The same rules are checked bit-exactly against the reference's
 // per-bit rules by the tests.
+// Warp `wic` of `wpc` writes the node groups r with r % wpc == wic.
 template <int W32>
 __device__ __forceinline__ void build_proposal(const uint32_t *rows,
                                                uint32_t *out, int n,
                                                const bbs_move_params &p,
                                                const uint32_t (&Dv)[W32],
                                                const uint32_t (&Dw)[W32],
-                                               bool related, int lane) {
+                                               bool related, int wpc, int wic,
+                                               int lane) {
   constexpr int RS = rs_of_w32(W32);
   const uint32_t v = p.v, w = p.w;
   uint32_t T1[W32], T2[W32];
@@ -318,7 +326,7 @@ __device__ __forceinline__ void build_proposal(const uint32_t *rows,
 #pragma unroll
   for (int r = 0; r < W32; r++) {
     const int x = 32 * r + lane;
-    if (x >= n) continue;
+    if (x >= n || r % wpc != wic) continue;
     const bool in_v = (Dv[r] >> lane) & 1u;
     const bool in_w = (Dw[r] >> lane) & 1u;
     uint32_t a[W32];
@@ -366,43 +374,68 @@ __device__ __forceinline__ void build_proposal(const uint32_t *rows,
 // ------------------------------------------------------------------------
 // Scoring (src/TreeScorer.hpp:131-210)
 // ------------------------------------------------------------------------
-// Exact int -> float for 0 <= n < 2^23 on the FP32/INT32 pipes.
-__device__ __forceinline__ float exact_float(int n) {
-  return __fsub_rn(__int_as_float(0x4B000000 + n), 8388608.0f);
-}
-
-// Per-(cell,node) score in the reference's order:
-// (((n00*l00 + n01*l01) + n10*l10) + n11*l11), no contraction.
-// From m = popc(M & A), k = popc(K & A): n11 = m, n01 = k - m,
-// n10 = popc(M) - m, n00 = popc(K) - popc(M) - k + m (M within K).
-__device__ __forceinline__ float pair_score(int k, int m, int pkm, int pm,
-                                            float l00, float l01, float l10,
-                                            float l11) {
-  const int n11 = m, n01 = k - m, n10 = pm - m, n00 = pkm - k + m;
-  float s = __fmul_rn(exact_float(n00), l00);
-  s = __fadd_rn(s, __fmul_rn(exact_float(n01), l01));
-  s = __fadd_rn(s, __fmul_rn(exact_float(n10), l10));
-  s = __fadd_rn(s, __fmul_rn(exact_float(n11), l11));
+// Population count of (X & A) over W32 words.  Groups of three words go
+// through a full adder (ones = a^b^c, twos = maj(a,b,c); both single LOP3
+// operations), so three words cost two POPC instead of three.
+template <int W32>
+__device__ __forceinline__ int masked_popc(const uint32_t (&X)[W32],
+                                          const uint32_t (&A)[W32]) {
+  int s = 0;
+  constexpr int G3 = W32 / 3;
+#pragma unroll
+  for (int g = 0; g < G3; g++) {
+    const uint32_t a = X[3 * g] & A[3 * g], b = X[3 * g + 1] & A[3 * g + 1],
+                   c = X[3 * g + 2] & A[3 * g + 2];
+    const uint32_t ones = a ^ b ^ c;
+    const uint32_t twos = (a & b) | (c & (a ^ b));
+    s += __popc(ones) + 2 * __popc(twos);
+  }
+#pragma unroll
+  for (int w = 3 * G3; w < W32; w++) s += __popc(X[w] & A[w]);
   return s;
 }
 
+// The per-(cell,node) score in the reference's order
+//   (((n00*l00 + n01*l01) + n10*l10) + n11*l11), no contraction,
+// with the four counts as exact floats.  With D = K & ~M (observed 0) and
+// M (observed 1), d = popc(D & A) and m = popc(M & A) give
+// n01 = d, n11 = m, n00 = popc(D) - d, n10 = popc(M) - m.  Biased floats
+// 2^23 + i (bit pattern 0x4B000000 + i) make every difference exact:
+//   pdb = 2^23 + popc(D),  pmb = 2^23 + popc(M).
+__device__ __forceinline__ float pair_score(int d, int m, float pdb,
+                                            float pmb, float l00, float l01,
+                                            float l10, float l11) {
+  const float db = __int_as_float(0x4B000000 + d);
+  const float mb = __int_as_float(0x4B000000 + m);
+  const float f01 = __fsub_rn(db, 8388608.0f);
+  const float f11 = __fsub_rn(mb, 8388608.0f);
+  const float f00 = __fsub_rn(pdb, db);
+  const float f10 = __fsub_rn(pmb, mb);
+  float s = __fmul_rn(f00, l00);
+  s = __fadd_rn(s, __fmul_rn(f01, l01));
+  s = __fadd_rn(s, __fmul_rn(f10, l10));
+  s = __fadd_rn(s, __fmul_rn(f11, l11));
+  return s;
+}
+
+// Per lane: Q cells as observed-0 rows D = K & ~M and observed-1 rows M.
 template <int W32, int Q>
 struct Cells {
-  uint32_t K[Q][W32], M[Q][W32];
-  int pkm[Q], pm[Q];
+  uint32_t D[Q][W32], M[Q][W32];
+  float pdb[Q], pmb[Q];
 };
 
-// Loads cells c = c0 + 32 q + lane (zero rows past n_cells: such a cell
-// has no counts and adds nothing).
+// Loads cells c = c0 + stride * q + lane (zero rows past n_cells: such a
+// cell has no counts and adds nothing).
 template <int W32, int Q>
 __device__ __forceinline__ void load_cells(Cells<W32, Q> &cb,
                                            const DatasetDev &ds, int c0,
-                                           int lane) {
+                                           int stride, int lane) {
   constexpr int RS = rs_of_w32(W32);
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    const int c = c0 + 32 * q + lane;
-    int pk = 0, pm = 0;
+    const int c = c0 + stride * q + lane;
+    int pd = 0, pm = 0;
 #pragma unroll
     for (int k = 0; k < W32; k++) {
       uint32_t kw = 0, mw = 0;
@@ -410,85 +443,111 @@ __device__ __forceinline__ void load_cells(Cells<W32, Q> &cb,
         kw = __ldg(ds.K + (size_t)c * RS + k);
         mw = __ldg(ds.M + (size_t)c * RS + k);
       }
-      cb.K[q][k] = kw;
+      cb.D[q][k] = kw & ~mw;
       cb.M[q][k] = mw;
-      pk += __popc(kw);
+      pd += __popc(kw & ~mw);
       pm += __popc(mw);
     }
-    cb.pkm[q] = pk - pm;
-    cb.pm[q] = pm;
+    cb.pdb[q] = __int_as_float(0x4B000000 + pd);
+    cb.pmb[q] = __int_as_float(0x4B000000 + pm);
   }
 }
 
-// Max-over-attachments for the lane's Q cells against all n ancestor rows;
-// returns the lane's sums of k and m at the first-max node (ties keep the
-// lower node, std::max in src/TreeScorer.hpp:187-193).
-template <int W32, int Q, bool ATTACH>
-__device__ __forceinline__ void score_cells(const uint32_t *rows, int n,
-                                            const Cells<W32, Q> &cb, float l00,
-                                            float l01, float l10, float l11,
-                                            int &sk, int &sm, int (&att)[Q]) {
+// First-max attachment node of each of the lane's Q cells against all n
+// ancestor rows (ties keep the lower node: std::max in
+// src/TreeScorer.hpp:187-193; node 0 always initialises).  Nodes are taken
+// two at a time for instruction-level parallelism, in order.
+template <int W32, int Q>
+__device__ __forceinline__ void best_nodes(const uint32_t *rows, int n,
+                                           const Cells<W32, Q> &cb, float l00,
+                                           float l01, float l10, float l11,
+                                           int (&bj)[Q]) {
   constexpr int RS = rs_of_w32(W32);
   float best[Q];
-  uint32_t bkm[Q];
   {
     uint32_t a[W32];
     ld_row<W32>(rows, a);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      int k = 0, m = 0;
-#pragma unroll
-      for (int w = 0; w < W32; w++) {
-        k += __popc(cb.K[q][w] & a[w]);
-        m += __popc(cb.M[q][w] & a[w]);
-      }
-      best[q] = pair_score(k, m, cb.pkm[q], cb.pm[q], l00, l01, l10, l11);
-      bkm[q] = (uint32_t)k | ((uint32_t)m << 16);
-      if constexpr (ATTACH) att[q] = 0;
+      const int d = masked_popc<W32>(cb.D[q], a);
+      const int m = masked_popc<W32>(cb.M[q], a);
+      best[q] = pair_score(d, m, cb.pdb[q], cb.pmb[q], l00, l01, l10, l11);
+      bj[q] = 0;
     }
   }
+  int j = 1;
 #pragma unroll 1
-  for (int j = 1; j < n; j++) {
+  for (; j + 1 < n; j += 2) {
+    uint32_t a[W32], b[W32];
+    ld_row<W32>(rows + j * RS, a);
+    ld_row<W32>(rows + (j + 1) * RS, b);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const float s0 = pair_score(masked_popc<W32>(cb.D[q], a),
+                                  masked_popc<W32>(cb.M[q], a), cb.pdb[q],
+                                  cb.pmb[q], l00, l01, l10, l11);
+      const float s1 = pair_score(masked_popc<W32>(cb.D[q], b),
+                                  masked_popc<W32>(cb.M[q], b), cb.pdb[q],
+                                  cb.pmb[q], l00, l01, l10, l11);
+      const bool up0 = s0 > best[q];
+      best[q] = up0 ? s0 : best[q];
+      bj[q] = up0 ? j : bj[q];
+      const bool up1 = s1 > best[q];
+      best[q] = up1 ? s1 : best[q];
+      bj[q] = up1 ? j + 1 : bj[q];
+    }
+  }
+  if (j < n) {
     uint32_t a[W32];
     ld_row<W32>(rows + j * RS, a);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      int k = 0, m = 0;
-#pragma unroll
-      for (int w = 0; w < W32; w++) {
-        k += __popc(cb.K[q][w] & a[w]);
-        m += __popc(cb.M[q][w] & a[w]);
-      }
-      const float s = pair_score(k, m, cb.pkm[q], cb.pm[q], l00, l01, l10, l11);
+      const float s = pair_score(masked_popc<W32>(cb.D[q], a),
+                                 masked_popc<W32>(cb.M[q], a), cb.pdb[q],
+                                 cb.pmb[q], l00, l01, l10, l11);
       const bool up = s > best[q];
       best[q] = up ? s : best[q];
-      bkm[q] = up ? ((uint32_t)k | ((uint32_t)m << 16)) : bkm[q];
-      if constexpr (ATTACH) att[q] = up ? j : att[q];
+      bj[q] = up ? j : bj[q];
     }
-  }
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    sk += (int)(bkm[q] & 0xffffu);
-    sm += (int)(bkm[q] >> 16);
   }
 }
 
-// Whole-tree class sums (warp-reduced) over all cell chunks.
+// Lane sums of k and m at the chosen nodes.
 template <int W32, int Q>
-__device__ __forceinline__ void score_tree(const uint32_t *rows, int n,
+__device__ __forceinline__ void counts_at(const uint32_t *rows,
+                                          const Cells<W32, Q> &cb,
+                                          const int (&bj)[Q], int &k, int &m) {
+  constexpr int RS = rs_of_w32(W32);
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    uint32_t a[W32];
+    ld_row<W32>(rows + bj[q] * RS, a);
+    const int mm = masked_popc<W32>(cb.M[q], a);
+    k += masked_popc<W32>(cb.D[q], a) + mm;
+    m += mm;
+  }
+}
+
+// This warp's part of the class sums over its cells.  Cells are split over
+// the `wpc` warps of a chain: cell = c0 + 32*wpc*q + 32*wic + lane.  With
+// `resident`, cb already holds the warp's cells.
+template <int W32, int Q>
+__device__ __forceinline__ void score_part(const uint32_t *rows, int n,
                                            const DatasetDev &ds,
                                            Cells<W32, Q> &cb, bool resident,
-                                           float l01, float l11, int lane,
-                                           int &sk, int &sm) {
-  int k = 0, m = 0, att[Q];
+                                           float l01, float l11, int wpc,
+                                           int wic, int lane, int &sk,
+                                           int &sm) {
+  int k = 0, m = 0, bj[Q];
   if (resident) {
-    score_cells<W32, Q, false>(rows, n, cb, ds.l00, l01, ds.l10, l11, k, m,
-                               att);
+    best_nodes<W32, Q>(rows, n, cb, ds.l00, l01, ds.l10, l11, bj);
+    counts_at<W32, Q>(rows, cb, bj, k, m);
   } else {
-    for (int c0 = 0; c0 < ds.n_cells; c0 += 32 * Q) {
-      load_cells<W32, Q>(cb, ds, c0, lane);
-      score_cells<W32, Q, false>(rows, n, cb, ds.l00, l01, ds.l10, l11, k, m,
-                                 att);
+    const int span = 32 * wpc * Q;
+    for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
+      load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
+      best_nodes<W32, Q>(rows, n, cb, ds.l00, l01, ds.l10, l11, bj);
+      counts_at<W32, Q>(rows, cb, bj, k, m);
     }
   }
   sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);

@@ -60,6 +60,7 @@ struct RunArgs {
   bbs_step_trace *trace;      // [n_chains][n_steps] or null
   const volatile int *cancel; // host-writable flag (mapped) or null
   int *status;                // device status word (0 = ok, 1 = cancelled)
+  int wpc;                    // warps per chain (cells split over them)
 };
 
 struct ScoreArgs {
@@ -94,13 +95,14 @@ struct GradArgs {
 };
 
 // Host launchers (bbs_kernels.cu).  Return a cudaError_t as int.
-int launch_mcmc(const RunArgs &a, int q, int warps_per_block, int n_sms,
+// chains_per_block must be 1 when a.wpc > 1 (the block is one chain).
+int launch_mcmc(const RunArgs &a, int q, int chains_per_block, int n_sms,
                 void *stream);
 int launch_score(const ScoreArgs &a, int q, void *stream);
 int launch_apply(const ApplyArgs &a, void *stream);
 int launch_grad(const GradArgs &a, int q, void *stream);
 int run_popc_bench(double *popc_per_s, double *clock_hz);
-size_t mcmc_smem_bytes(int n_nodes, int warps_per_block);
+size_t mcmc_smem_bytes(int n_nodes, int wpc, int chains_per_block);
 int pick_q(int n_cells);
 
 }  // namespace bbs

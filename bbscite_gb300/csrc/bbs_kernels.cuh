@@ -1,9 +1,11 @@
 // bbs_kernels.cuh -- kernel templates of the GB300 path.
 //
-//   mcmc_kernel   persistent chain runner: one warp per chain, the chain's
-//                 current and proposed ancestor rows double-buffered in
-//                 shared memory, cell rows in registers (or re-read per
-//                 chunk for wide datasets); src/Application.hpp:398-496.
+//   mcmc_kernel   persistent chain runner, src/Application.hpp:398-496.
+//                 A chain is one warp, or `wpc` warps that split its cells
+//                 (the block is then that one chain).  The chain's current
+//                 and proposed ancestor rows are double-buffered in shared
+//                 memory; cell rows stay in registers (or are re-read per
+//                 chunk for wide datasets).
 //   score_kernel  TreeScorer::logscore_tree over a batch (warp per tree).
 //   apply_kernel  realize_raw_move_sample + update ctor over a batch.
 //   grad_kernel   sum-over-attachments score with its fused adjoint.
@@ -16,39 +18,70 @@
 
 namespace bbs {
 
+// Rows x = 32 r + lane for the node groups r owned by warp `wic` of `wpc`.
 template <int W32>
-__device__ __forceinline__ void copy_rows(const uint32_t *src, uint32_t *dst,
-                                          int n, int lane) {
+__device__ __forceinline__ void copy_rows_part(const uint32_t *src,
+                                               uint32_t *dst, int n, int wpc,
+                                               int wic, int lane) {
   constexpr int RS = rs_of_w32(W32);
-  for (int x = lane; x < n; x += 32) {
-    uint32_t r[W32];
-    ld_row<W32>(src + x * RS, r);
-    st_row<W32>(dst + x * RS, r);
+  for (int r = wic; r < W32; r += wpc) {
+    const int x = 32 * r + lane;
+    if (x < n) {
+      uint32_t v[W32];
+      ld_row<W32>(src + x * RS, v);
+      st_row<W32>(dst + x * RS, v);
+    }
   }
 }
 
+template <int W32>
+__device__ __forceinline__ void copy_rows(const uint32_t *src, uint32_t *dst,
+                                          int n, int lane) {
+  copy_rows_part<W32>(src, dst, n, 1, 0, lane);
+}
+
+// Shared-memory words per chain slot: two row buffers, the partial class
+// sums of both step parities (2 x wpc x 2 ints) and a flag word, padded to
+// 16 bytes.
+__host__ __device__ inline int slot_words(int n, int rs, int wpc) {
+  return 2 * n * rs + 4 * wpc + 4;
+}
+
+// Resident 128-thread blocks per SM the register budget aims for: fewer
+// cells per lane leave room for more warps.
 template <int W32, int Q>
-__global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
+struct McmcOccupancy {
+  static constexpr int min_blocks = Q == 1 ? 4 : (Q == 2 ? 3 : 2);
+};
+
+template <int W32, int Q>
+__global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
+    mcmc_kernel(const RunArgs a) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int RS = rs_of_w32(W32);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
+  const int wpc = a.wpc;
+  const int cpb = wpb / wpc;
+  const int slot = wib / wpc, wic = wib - slot * wpc;
   const int n = a.ds.n_nodes;
-  uint32_t *buf0 = smem + (size_t)wib * 2 * n * RS;
+  uint32_t *buf0 = smem + (size_t)slot * slot_words(n, RS, wpc);
   uint32_t *buf1 = buf0 + n * RS;
-  const int total_warps = gridDim.x * wpb;
-  const bool resident = a.ds.n_cells <= 32 * Q;
+  int *part = reinterpret_cast<int *>(buf0 + 2 * n * RS);
+  volatile int *sflag = part + 4 * wpc;
+  const bool multi = wpc > 1;  // block-uniform
+  const bool resident = a.ds.n_cells <= 32 * wpc * Q;
   Cells<W32, Q> cb;
-  if (resident) load_cells<W32, Q>(cb, a.ds, 0, lane);
+  if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
 
-  for (int chain = blockIdx.x * wpb + wib; chain < a.n_chains;
-       chain += total_warps) {
+  for (int chain = blockIdx.x * cpb + slot; chain < a.n_chains;
+       chain += gridDim.x * cpb) {
     const ChainState st = a.states[chain];
     uint32_t *g = a.rows + (size_t)chain * n * RS;
     uint32_t *gbest = a.best_rows + (size_t)chain * n * RS;
-    copy_rows<W32>(g, buf0, n, lane);
-    __syncwarp();
+    copy_rows_part<W32>(g, buf0, n, wpc, wic, lane);
+    if (multi) __syncthreads(); else __syncwarp();
     uint32_t *cur = buf0, *prop = buf1;
     float beta = st.beta, score = st.score;
     float l01 = st.l01, l11 = st.l11, prior = st.prior;
@@ -60,9 +93,11 @@ __global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
     bool cancelled = false;
     for (; i < a.n_steps; i++) {
       if (a.cancel != nullptr && (i & 255) == 0) {
-        int c = 0;
-        if (lane == 0) c = *a.cancel;
-        c = __shfl_sync(BBS_FULL_MASK, c, 0);
+        // one reader, then a chain-uniform decision
+        if (wic == 0 && lane == 0) *sflag = *a.cancel;
+        if (multi) __syncthreads(); else __syncwarp();
+        const int c = *sflag;
+        if (multi) __syncthreads(); else __syncwarp();
         if (c) {
           cancelled = true;
           break;
@@ -70,9 +105,10 @@ __global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
       }
       const uint64_t step = st.steps_done + (uint64_t)i;
       const bbs_raw_move raw =
-          a.moves != nullptr ? a.moves[(size_t)chain * a.n_steps + i]
-                             : sample_move(a.mp, (uint32_t)n, a.seed,
-                                           (uint32_t)chain, step);
+          a.moves != nullptr
+              ? a.moves[(size_t)chain * a.n_steps + i]
+              : sample_move(a.mp, (uint32_t)n, a.seed, (uint32_t)chain, step,
+                            a.trace != nullptr);
       uint32_t Dv[W32], Dw[W32];
       const Realized R = realize_move<W32>(cur, n, beta, raw, lane, Dv, Dw);
       const bool beta_move = raw.move_type == BBS_MOVE_CHANGE_BETA;
@@ -82,13 +118,27 @@ __global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
         pbeta = R.p.new_beta;
         beta_terms(a.ds, pbeta, pl01, pl11, pprior);
       } else {
-        build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, lane);
+        build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
+                            lane);
         scored = prop;
       }
-      __syncwarp();
+      if (multi) __syncthreads(); else __syncwarp();
       int sk, sm;
-      score_tree<W32, Q>(scored, n, a.ds, cb, resident, pl01, pl11, lane, sk,
-                         sm);
+      score_part<W32, Q>(scored, n, a.ds, cb, resident, pl01, pl11, wpc, wic,
+                         lane, sk, sm);
+      if (multi) {
+        int *pp = part + (i & 1) * 2 * wpc;
+        if (lane == 0) {
+          pp[2 * wic] = sk;
+          pp[2 * wic + 1] = sm;
+        }
+        __syncthreads();
+        sk = sm = 0;
+        for (int w = 0; w < wpc; w++) {
+          sk += pp[2 * w];
+          sm += pp[2 * w + 1];
+        }
+      }
       const float pscore = tree_score(a.ds, sk, sm, pl01, pl11, pprior);
       // src/Application.hpp:443-456
       float corr = 1.0f;
@@ -103,9 +153,9 @@ __global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
         best_beta = pbeta;
         bsk = sk;
         bsm = sm;
-        copy_rows<W32>(scored, gbest, n, lane);
+        copy_rows_part<W32>(scored, gbest, n, wpc, wic, lane);
       }
-      if (a.trace != nullptr && lane == 0) {
+      if (a.trace != nullptr && wic == 0 && lane == 0) {
         bbs_step_trace *t = a.trace + (size_t)chain * a.n_steps + i;
         t->move = raw;
         t->proposed_score = pscore;
@@ -133,8 +183,8 @@ __global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
       }
       __syncwarp();
     }
-    copy_rows<W32>(cur, g, n, lane);
-    if (lane == 0) {
+    copy_rows_part<W32>(cur, g, n, wpc, wic, lane);
+    if (wic == 0 && lane == 0) {
       ChainState o = st;
       o.beta = beta;
       o.score = score;
@@ -152,7 +202,7 @@ __global__ void __launch_bounds__(128) mcmc_kernel(const RunArgs a) {
       a.states[chain] = o;
       if (cancelled && a.status != nullptr) atomicOr(a.status, 1);
     }
-    __syncwarp();
+    if (multi) __syncthreads(); else __syncwarp();
   }
 }
 
@@ -173,16 +223,16 @@ __global__ void __launch_bounds__(128) score_kernel(const ScoreArgs a) {
   Cells<W32, Q> cb;
   int k = 0, m = 0;
   for (int c0 = 0; c0 < a.ds.n_cells; c0 += 32 * Q) {
-    load_cells<W32, Q>(cb, a.ds, c0, lane);
-    int att[Q];
-    score_cells<W32, Q, ATTACH>(rows, n, cb, a.ds.l00, l01, a.ds.l10, l11, k,
-                                m, att);
+    load_cells<W32, Q>(cb, a.ds, c0, 32, lane);
+    int bj[Q];
+    best_nodes<W32, Q>(rows, n, cb, a.ds.l00, l01, a.ds.l10, l11, bj);
+    counts_at<W32, Q>(rows, cb, bj, k, m);
     if constexpr (ATTACH) {
 #pragma unroll
       for (int q = 0; q < Q; q++) {
         const int c = c0 + 32 * q + lane;
         if (c < a.ds.n_cells)
-          a.attach[(size_t)tree * a.ds.n_cells + c] = (uint32_t)att[q];
+          a.attach[(size_t)tree * a.ds.n_cells + c] = (uint32_t)bj[q];
       }
     }
   }
@@ -245,7 +295,7 @@ __global__ void __launch_bounds__(128) apply_kernel(const ApplyArgs a) {
     related = has_bit<W32>(Dw, p.v);
   }
   uint32_t *out = a.rows_out + (size_t)tree * n * RS;
-  build_proposal<W32>(rows, out, n, p, Dv, Dw, related, lane);
+  build_proposal<W32>(rows, out, n, p, Dv, Dw, related, 1, 0, lane);
   if (lane == 0) {
     if (a.params_out) a.params_out[tree] = p;
     if (a.beta_out)
@@ -275,7 +325,7 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradArgs a) {
         acc_n11 = 0.0f;
   Cells<W32, Q> cb;
   for (int c0 = 0; c0 < a.ds.n_cells; c0 += 32 * Q) {
-    load_cells<W32, Q>(cb, a.ds, c0, lane);
+    load_cells<W32, Q>(cb, a.ds, c0, 32, lane);
     float mx[Q], z[Q], ek[Q], em[Q];
 #pragma unroll
     for (int q = 0; q < Q; q++) {
@@ -287,13 +337,10 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradArgs a) {
       ld_row<W32>(rows + j * RS, r);
 #pragma unroll
       for (int q = 0; q < Q; q++) {
-        int k = 0, m = 0;
-#pragma unroll
-        for (int w = 0; w < W32; w++) {
-          k += __popc(cb.K[q][w] & r[w]);
-          m += __popc(cb.M[q][w] & r[w]);
-        }
-        const float s = pair_score(k, m, cb.pkm[q], cb.pm[q], l00, l01, l10, l11);
+        const int d = masked_popc<W32>(cb.D[q], r);
+        const int m = masked_popc<W32>(cb.M[q], r);
+        const int k = d + m;
+        const float s = pair_score(d, m, cb.pdb[q], cb.pmb[q], l00, l01, l10, l11);
         if (s > mx[q]) {
           const float sc = expf(mx[q] - s);
           z[q] = z[q] * sc + 1.0f;
@@ -314,24 +361,21 @@ __global__ void __launch_bounds__(128) grad_kernel(const GradArgs a) {
       if (c >= a.ds.n_cells) continue;
       const float lse = mx[q] + logf(z[q]);
       const float Ek = ek[q] / z[q], Em = em[q] / z[q];
-      const float pk = (float)(cb.pkm[q] + cb.pm[q]), pm = (float)cb.pm[q];
+      const float pm = cb.pmb[q] - 8388608.0f;
+      const float pkm = cb.pdb[q] - 8388608.0f;
       acc_lse += lse;
       acc_n11 += Em;
       acc_n01 += Ek - Em;
       acc_n10 += pm - Em;
-      acc_n00 += (pk - pm) - Ek + Em;
+      acc_n00 += pkm - Ek + Em;
       if (a.posterior != nullptr) {
         float *post = a.posterior + ((size_t)tree * a.ds.n_cells + c) * n;
         for (int j = 0; j < n; j++) {
           uint32_t r[W32];
           ld_row<W32>(rows + j * RS, r);
-          int k = 0, m = 0;
-#pragma unroll
-          for (int w = 0; w < W32; w++) {
-            k += __popc(cb.K[q][w] & r[w]);
-            m += __popc(cb.M[q][w] & r[w]);
-          }
-          const float s = pair_score(k, m, cb.pkm[q], cb.pm[q], l00, l01, l10, l11);
+          const float s = pair_score(masked_popc<W32>(cb.D[q], r),
+                                     masked_popc<W32>(cb.M[q], r), cb.pdb[q],
+                                     cb.pmb[q], l00, l01, l10, l11);
           post[j] = expf(s - lse);
         }
       }

@@ -15,28 +15,33 @@ inline cudaError_t prepare_smem(K kernel, size_t smem) {
   return cudaSuccess;
 }
 
-// Persistent launch: as many warps as chains, capped at what stays
-// resident, so each warp walks chain, chain + total_warps, ...
+// Persistent launch.  wpc == 1: blocks of `cpb` one-warp chains; wpc > 1:
+// blocks of one chain of wpc warps.  As many blocks as chains need, capped
+// at what stays resident; each block then walks its chain slots.
 template <int W32, int Q>
-int launch_mcmc_t(const RunArgs &a, int wpb, int n_sms, cudaStream_t s) {
+int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
-  const size_t smem = (size_t)wpb * 2 * a.ds.n_nodes * RS * sizeof(uint32_t);
+  if (a.wpc > 1) cpb = 1;
+  const int threads = 32 * a.wpc * cpb;
+  if (threads > 128) return (int)cudaErrorInvalidConfiguration;
+  const size_t smem =
+      (size_t)cpb * slot_words(a.ds.n_nodes, RS, a.wpc) * sizeof(uint32_t);
   cudaError_t e = prepare_smem(mcmc_kernel<W32, Q>, smem);
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mcmc_kernel<W32, Q>,
-                                                    wpb * 32, smem);
+                                                    threads, smem);
   if (e != cudaSuccess) return (int)e;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
-  const int want = (a.n_chains + wpb - 1) / wpb;
+  const int want = (a.n_chains + cpb - 1) / cpb;
   const int blocks = std::max(1, std::min(want, per_sm * n_sms));
-  mcmc_kernel<W32, Q><<<blocks, wpb * 32, smem, s>>>(a);
+  mcmc_kernel<W32, Q><<<blocks, threads, smem, s>>>(a);
   return (int)cudaGetLastError();
 }
 
-int launch_mcmc_lo(const RunArgs &a, int w32, int q, int wpb, int n_sms,
+int launch_mcmc_lo(const RunArgs &a, int w32, int q, int cpb, int n_sms,
                    cudaStream_t s);
-int launch_mcmc_hi(const RunArgs &a, int w32, int q, int wpb, int n_sms,
+int launch_mcmc_hi(const RunArgs &a, int w32, int q, int cpb, int n_sms,
                    cudaStream_t s);
 
 }  // namespace bbs

@@ -4,12 +4,12 @@
 namespace bbs {
 
 #define BBS_Q_CASES(W)                                        \
-  case W * 10 + 1: return launch_mcmc_t<W, 1>(a, wpb, n_sms, s); \
-  case W * 10 + 2: return launch_mcmc_t<W, 2>(a, wpb, n_sms, s); \
-  case W * 10 + 3: return launch_mcmc_t<W, 3>(a, wpb, n_sms, s); \
-  case W * 10 + 4: return launch_mcmc_t<W, 4>(a, wpb, n_sms, s);
+  case W * 10 + 1: return launch_mcmc_t<W, 1>(a, cpb, n_sms, s); \
+  case W * 10 + 2: return launch_mcmc_t<W, 2>(a, cpb, n_sms, s); \
+  case W * 10 + 3: return launch_mcmc_t<W, 3>(a, cpb, n_sms, s); \
+  case W * 10 + 4: return launch_mcmc_t<W, 4>(a, cpb, n_sms, s);
 
-int launch_mcmc_lo(const RunArgs &a, int w32, int q, int wpb, int n_sms,
+int launch_mcmc_lo(const RunArgs &a, int w32, int q, int cpb, int n_sms,
                    cudaStream_t s) {
   switch (w32 * 10 + q) {
     BBS_Q_CASES(1)

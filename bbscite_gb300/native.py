@@ -85,6 +85,9 @@ def lib():
         "bbs_sync": (C.c_int, [v]),
         "bbs_cancel": (C.c_int, [v]),
         "bbs_last_run_ms": (C.c_int, [v, v]),
+        "bbs_set_launch": (C.c_int, [v, C.c_int, C.c_int, C.c_int]),
+        "bbs_get_launch": (C.c_int, [v, v, v, v]),
+        "bbs_autotune": (C.c_int, [v, u32, v]),
         "bbs_get_best": (C.c_int, [v, v, v, v, v, v, v, v]),
         "bbs_get_chains": (C.c_int, [v, v, v, v, v]),
         "bbs_score_trees": (C.c_int, [v, v, v, u32, v, v, v]),
@@ -252,6 +255,22 @@ class Context:
 
     def cancel(self) -> None:
         check(lib().bbs_cancel(self._h))
+
+    def set_launch(self, cells_per_lane=0, warps_per_chain=0,
+                   chains_per_block=0) -> None:
+        check(lib().bbs_set_launch(self._h, cells_per_lane, warps_per_chain,
+                                   chains_per_block))
+
+    def launch(self) -> tuple:
+        q, w, b = C.c_int(), C.c_int(), C.c_int()
+        check(lib().bbs_get_launch(self._h, C.byref(q), C.byref(w),
+                                   C.byref(b)))
+        return q.value, w.value, b.value
+
+    def autotune(self, probe_steps: int = 64) -> float:
+        ms = C.c_float()
+        check(lib().bbs_autotune(self._h, probe_steps, C.byref(ms)))
+        return ms.value
 
     def last_run_ms(self) -> float:
         """Device time of the last run (CUDA events on the context's

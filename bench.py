@@ -66,6 +66,10 @@ def parse_args(argv=None):
                     help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--autotune", type=int, default=1)
+    ap.add_argument("--autotune-steps", type=int, default=200)
+    ap.add_argument("--launch", default="",
+                    help="cells_per_lane,warps_per_chain,chains_per_block")
     return ap.parse_args(argv)
 
 
@@ -257,6 +261,12 @@ def run_ours(args) -> None:
                               seed=0xB5C17E + rank)
     ctx = N.Context(mut, known, Cn, G, params)
     ctx.init_chains(chains)
+    # launch shape from the autotuner (chain state is restored afterwards)
+    if args.launch:
+        ctx.set_launch(*[int(x) for x in args.launch.split(",")])
+    elif args.autotune:
+        ctx.autotune(args.autotune_steps)
+    shape = ctx.launch()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
 
     for _ in range(args.warmup):
@@ -302,6 +312,7 @@ def run_ours(args) -> None:
         c2 = N.Context(mut, known, Cn, G, params)
         parents = N.random_parents(params.seed, G, chains)
         c2.init_chains(chains, parents)
+        c2.set_launch(*shape)
         c2.run(L)
         b2 = c2.best()
         c2.close()
@@ -323,6 +334,10 @@ def run_ours(args) -> None:
                         " fixed error rates alpha=1e-3 beta=0.2, Philox moves",
             "n_genes": G, "n_cells": Cn, "chains": chains,
             "chain_steps_per_launch": L, "parallelism": f"replicas x{ws}",
+            "launch": {"cells_per_lane": shape[0],
+                       "warps_per_chain": shape[1],
+                       "chains_per_block": shape[2],
+                       "autotuned": bool(args.autotune)},
             "l2": "256 MiB buffer written between launches",
         },
         "roofline": {

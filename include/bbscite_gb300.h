@@ -171,6 +171,20 @@ BBS_API int bbs_sync(bbs_ctx *ctx);
  * returns BBS_ERR_TIMEOUT.  Safe from another host thread. */
 BBS_API int bbs_cancel(bbs_ctx *ctx);
 
+/* Launch shape of the chain kernel (no counterpart in the reference, whose
+ * FPGA pipeline has a fixed chain-group size, src/main.cpp:28-32):
+ * cells per lane per chunk (1-4; 1-2 above 128 nodes), warps per chain
+ * (1-4; the cells are split over them) and chains per block (one-warp
+ * chains only).  0 keeps a value.  bbs_init_chains picks a default. */
+BBS_API int bbs_set_launch(bbs_ctx *ctx, int cells_per_lane,
+                           int warps_per_chain, int chains_per_block);
+BBS_API int bbs_get_launch(const bbs_ctx *ctx, int *cells_per_lane,
+                           int *warps_per_chain, int *chains_per_block);
+/* Times probe_steps steps of every launch shape on the current chains
+ * (their state is restored afterwards) and keeps the fastest; best_ms
+ * (optional) receives its time. */
+BBS_API int bbs_autotune(bbs_ctx *ctx, uint32_t probe_steps, float *best_ms);
+
 /* Device time in milliseconds of the last completed bbs_run / bbs_sync,
  * measured with CUDA events recorded on the context's stream around the
  * chain kernel (src/Application.hpp:197-219 reports the kernel makespan). */

@@ -346,3 +346,50 @@ def test_sumscore_grad_vs_fp64(native, orc):
                 np.testing.assert_allclose(post[t].sum(axis=1), 1.0,
                                            rtol=1e-4)
     c.close()
+
+
+@pytest.mark.parametrize("G,Cn", [(95, 96), (40, 200), (127, 64), (200, 150)])
+def test_launch_shapes_give_identical_chains(native, orc, G, Cn):
+    """Every launch shape (cells per lane, warps per chain, chains per
+    block) computes the same chains bit for bit."""
+    m, _, _ = D.generate_dataset(G + 3 * Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    shapes = [(1, 1, 1), (2, 1, 2), (1, 2, 1), (1, 3, 1), (2, 2, 1),
+              (1, 4, 1), (2, 1, 4)]
+    qmax = 2 if G + 1 > 128 else 4
+    outs = []
+    for q, wpc, cpb in shapes:
+        if q > qmax:
+            continue
+        p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=31,
+                                  prob_beta_change=0.05)
+        with native.Context(mut, known, Cn, G, p) as c:
+            c.init_chains(9)
+            c.set_launch(q, wpc, cpb)
+            tr = c.run(150, trace=True)
+            outs.append((c.chains(), c.best(), tr))
+    ch0, b0, t0 = outs[0]
+    for ch, b, t in outs[1:]:
+        assert (ch["dm"] == ch0["dm"]).all()
+        np.testing.assert_array_equal(ch["score"], ch0["score"])
+        assert b["score"] == b0["score"] and (b["dm"] == b0["dm"]).all()
+        assert (t["accepted"] == t0["accepted"]).all()
+        assert (t["proposed_counts"] == t0["proposed_counts"]).all()
+
+
+def test_autotune_keeps_chain_state(native):
+    m, _, _ = D.generate_dataset(8, 60, 80, 1e-3, 0.2, 0.1, 0.0)
+    mut, known = D.matrix_to_bits(m)
+    p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=5)
+    with native.Context(mut, known, 80, 60, p) as c:
+        c.init_chains(16)
+        c.run(100)
+        before = c.chains()
+        ms = c.autotune(32)
+        assert ms > 0
+        after = c.chains()
+        assert (before["dm"] == after["dm"]).all()
+        np.testing.assert_array_equal(before["score"], after["score"])
+        q, wpc, cpb = c.launch()
+        assert 1 <= q <= 4 and 1 <= wpc <= 4 and 1 <= cpb <= 4
+        c.run(50)  # continues from the saved state
