@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <mutex>
 #include <new>
 #include <sstream>
 #include <string>
@@ -1139,3 +1140,94 @@ int bbs_popc_peak(double *popc_per_s, double *sm_clock_hz) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Allocation-free scoring.  The per-tree log-table scratch of
+// bbs_score_trees (beta, log beta, log(1-beta), Beta prior) lives in this
+// file-scope device array instead of a cudaMalloc'd buffer.  Host code may
+// not use the array's name as a device address: the address is looked up
+// once per device with cudaGetSymbolAddress, with that device current, and
+// passed to the kernel.  Each call overwrites the entries of its own trees
+// before the kernel reads them, so nothing in the array has to start at
+// zero.
+// ------------------------------------------------------------------------
+static __device__ __align__(256) float g_noalloc_terms[BBS_NOALLOC_MAX_TREES * 4];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+float *g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of g_noalloc_terms on the current device (set up on the
+// first call per device).
+int noalloc_scratch(int device, float **out) {
+  if (device < 0 || device >= kNoallocMaxDevices)
+    return fail(BBS_ERR_SIZE, "device ordinal %d is not supported", device);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_ptr[device] == nullptr) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_terms);
+    if (e != cudaSuccess)
+      return cuda_fail((int)e, "cudaGetSymbolAddress(scratch)");
+    g_noalloc_ptr[device] = static_cast<float *>(ptr);
+  }
+  *out = g_noalloc_ptr[device];
+  return BBS_OK;
+}
+
+}  // namespace
+
+extern "C" int bbs_score_trees_noalloc(bbs_ctx *c, const uint64_t *dm_device,
+                                       const float *betas, uint32_t n_trees,
+                                       float *scores_device,
+                                       uint64_t *counts_device) {
+  if (!c || !dm_device || !betas || !scores_device)
+    return fail(BBS_ERR_INPUT, "NULL argument to bbs_score_trees_noalloc");
+  if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+  if (n_trees == 0) return BBS_OK;
+  if (n_trees > BBS_NOALLOC_MAX_TREES)
+    return fail(BBS_ERR_SIZE,
+                "bbs_score_trees_noalloc takes at most %d trees per call "
+                "(got %u): its scratch is a fixed %d-entry device array",
+                BBS_NOALLOC_MAX_TREES, n_trees, BBS_NOALLOC_MAX_TREES);
+  for (uint32_t t = 0; t < n_trees; t++)
+    if (!(betas[t] > 0.0f && betas[t] < 1.0f))
+      return fail(BBS_ERR_INPUT, "beta of tree %u outside (0, 1)", t);
+  int device = -1;
+  BBS_CUDA(cudaGetDevice(&device), "cudaGetDevice");
+  if (device != c->device)
+    return fail(BBS_ERR_STATE, "the context's device %d is not current (%d)",
+                c->device, device);
+  float *scratch = nullptr;
+  int r = noalloc_scratch(device, &scratch);
+  if (r != BBS_OK) return r;
+  // Host log-table terms, staged through a fixed stack buffer.
+  constexpr uint32_t kChunk = 512;
+  float chunk[4 * kChunk];
+  for (uint32_t t0 = 0; t0 < n_trees; t0 += kChunk) {
+    const uint32_t nt = std::min(kChunk, n_trees - t0);
+    for (uint32_t t = 0; t < nt; t++) {
+      chunk[4 * t] = betas[t0 + t];
+      host_beta_terms(c->ds, betas[t0 + t], &chunk[4 * t + 1],
+                      &chunk[4 * t + 2], &chunk[4 * t + 3]);
+    }
+    BBS_CUDA(cudaMemcpyAsync(scratch + 4 * (size_t)t0, chunk,
+                             sizeof(float) * 4 * nt, cudaMemcpyHostToDevice,
+                             c->stream),
+             "scratch upload");
+  }
+  ScoreArgs a{};
+  a.ds = c->ds;
+  a.rows = reinterpret_cast<const uint32_t *>(dm_device);
+  a.beta_terms = scratch;
+  a.n_trees = (int)n_trees;
+  a.scores = scores_device;
+  a.counts = counts_device;
+  a.attach = nullptr;
+  a.states = nullptr;
+  const int e = launch_score(a, c->q, c->stream);
+  if (e != 0) return cuda_fail(e, "score kernel launch");
+  return sync_stream(c, "score kernel");
+}
+

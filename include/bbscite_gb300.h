@@ -230,6 +230,28 @@ BBS_API int bbs_sumscore_grad(bbs_ctx *ctx, const uint64_t *dm, const float *alp
                       const float *betas, uint32_t n_trees, float *logl,
                       float *dalpha, float *dbeta, float *posterior);
 
+/* bbs_score_trees for callers that cannot allocate GPU memory (no
+ * counterpart in the reference).  Some callers cannot call cudaMalloc at
+ * scoring time: a framework that has handed all device memory to its own
+ * pool, a latency-critical loop where an allocation would synchronise the
+ * device, or code that must leave the allocator untouched between set-up
+ * and teardown.  This entry point allocates nothing.  The caller passes
+ * device buffers: dm_device (n_trees x n_nodes x W ancestor rows),
+ * scores_device (n_trees floats) and counts_device (n_trees x 4, may be
+ * NULL), plus the betas in host memory.  The per-tree log-table scratch
+ * lives in a fixed device array of BBS_NOALLOC_MAX_TREES entries (256 KB),
+ * which every GPU that loads this library holds until the process exits;
+ * more trees per call are rejected with BBS_ERR_SIZE.  The first call on a
+ * device looks that array's address up (cudaGetSymbolAddress); make it
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (several host threads or contexts at once) race;
+ * serialise them.  The context's device must be the current device. */
+#define BBS_NOALLOC_MAX_TREES 16384
+BBS_API int bbs_score_trees_noalloc(bbs_ctx *ctx, const uint64_t *dm_device,
+                                    const float *betas, uint32_t n_trees,
+                                    float *scores_device,
+                                    uint64_t *counts_device);
+
 /* Integer-pipe calibration: 32-bit POPC throughput of this device in
  * operations per second (a timed microbenchmark). */
 BBS_API int bbs_popc_peak(double *popc_per_s, double *sm_clock_hz);
