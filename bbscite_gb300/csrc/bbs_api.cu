@@ -216,9 +216,12 @@ struct bbs_ctx {
   uint32_t n_cells = 0, n_genes = 0, n_nodes = 0, W64 = 0, RS = 0;
   bbs_params params{};
   DatasetDev ds{};
-  MoveProbs mp{};
-  float l01_0 = 0, l11_0 = 0, prior_0 = 0;  // terms of beta_mean (host libm)
+  ModelDev md{};
+  float terms[8] = {};  // (alpha_mean, beta_mean) log-table terms, host libm
   uint32_t *d_K = nullptr, *d_M = nullptr;
+  DatasetDev *d_ds = nullptr;  // one-entry tables for the init kernel
+  ModelDev *d_md = nullptr;
+  float *d_terms = nullptr;
   uint32_t n_chains = 0;
   uint32_t *d_rows = nullptr, *d_best = nullptr;
   ChainState *d_states = nullptr;
@@ -269,7 +272,82 @@ int check_params(const bbs_params *p) {
   if (!(p->beta_mean > 0.0f && p->beta_mean < 1.0f))
     return fail(BBS_ERR_INPUT, "beta must lie in (0, 1), got %g", p->beta_mean);
   if (!(p->beta_sd > 0.0f)) return fail(BBS_ERR_INPUT, "beta_sd must be positive");
+  if (p->score_mode > BBS_SCORE_SUM)
+    return fail(BBS_ERR_INPUT, "unknown score mode %u", p->score_mode);
+  if (p->error_move > BBS_ERROR_LANGEVIN)
+    return fail(BBS_ERR_INPUT, "unknown error move %u", p->error_move);
+  if (p->error_move != BBS_ERROR_BETA_WALK && !(p->error_step > 0.0f))
+    return fail(BBS_ERR_INPUT, "error_step must be positive");
   return BBS_OK;
+}
+
+// Host side of one dataset: cell rows (genes only, mutated within known),
+// the scorer constants of src/TreeScorer.hpp:99-111, the move thresholds of
+// src/Parameters.hpp:451-584 / src/RawMoveDistribution.hpp:119-131 and the
+// log-table terms of (alpha_mean, beta_mean).  Device pointers are filled
+// in by the caller.
+struct HostDataset {
+  std::vector<uint64_t> K, M;
+  DatasetDev ds{};
+  ModelDev md{};
+  float terms[8] = {};
+};
+
+void prepare_dataset(const bbs_params *params, uint32_t n_cells,
+                     uint32_t n_genes, const uint64_t *is_mutated,
+                     const uint64_t *is_known, HostDataset &h) {
+  const uint32_t n_nodes = n_genes + 1, W64 = words64(n_nodes);
+  h.K.assign((size_t)n_cells * W64, 0);
+  h.M.assign(h.K.size(), 0);
+  int64_t sum_k = 0, sum_m = 0;
+  for (uint32_t cell = 0; cell < n_cells; cell++)
+    for (uint32_t k = 0; k < W64; k++) {
+      uint64_t mask = ~0ull;
+      const uint32_t lo = 64 * k;
+      if (lo >= n_genes) mask = 0;
+      else if (n_genes - lo < 64) mask = (1ull << (n_genes - lo)) - 1ull;
+      const size_t i = (size_t)cell * W64 + k;
+      h.K[i] = is_known[i] & mask;
+      h.M[i] = is_mutated[i] & h.K[i];
+      sum_k += __builtin_popcountll(h.K[i]);
+      sum_m += __builtin_popcountll(h.M[i]);
+    }
+  const float alpha = params->alpha_mean, bm = params->beta_mean,
+              sd = params->beta_sd;
+  DatasetDev &ds = h.ds;
+  ds.n_cells = (int)n_cells;
+  ds.n_nodes = (int)n_nodes;
+  ds.sum_k = (int)sum_k;
+  ds.sum_m = (int)sum_m;
+  ds.l00 = (float)std::log(1.0 - (double)alpha);
+  ds.l10 = logf(alpha);
+  ds.bpa = (float)(((double)(1.0f - bm) * std::pow((double)bm, 2.0) /
+                    std::pow((double)sd, 2.0)) - (double)bm);
+  ds.bpb = ds.bpa * ((1.0f / bm) - 1.0f);
+  ds.lg_ab = logf(tgammaf(ds.bpa + ds.bpb));
+  ds.lg_a = logf(tgammaf(ds.bpa));
+  ds.lg_b = logf(tgammaf(ds.bpb));
+  const float sum = params->prob_beta_change + params->prob_prune_n_reattach +
+                    params->prob_swap_nodes + params->prob_swap_subtrees;
+  const float pb = params->prob_beta_change / sum;
+  const float pp = params->prob_prune_n_reattach / sum;
+  const float ps = params->prob_swap_nodes / sum;
+  ModelDev &md = h.md;
+  md.mp.cum_beta = pb;
+  md.mp.cum_prune = pb + pp;
+  md.mp.cum_swap = pb + pp + ps;
+  md.mp.beta_jump_sd = sd / params->beta_jump_scaling_chi;
+  md.gamma = params->gamma;
+  md.score_mode = (int32_t)params->score_mode;
+  md.error_move = (int32_t)params->error_move;
+  md.error_step = params->error_step;
+  md.seed = params->seed;
+  h.terms[0] = alpha;
+  h.terms[1] = bm;
+  h.terms[2] = ds.l00;
+  h.terms[3] = ds.l10;
+  host_beta_terms(ds, bm, &h.terms[4], &h.terms[5], &h.terms[6]);
+  h.terms[7] = 0.0f;
 }
 
 int sync_stream(bbs_ctx *c, const char *what) {
@@ -306,6 +384,9 @@ void bbs_params_default(bbs_params *p) {
   p->beta_jump_scaling_chi = 10.0f;
   p->gamma = 1.0f;
   p->seed = 0x5eed5eedull;
+  p->score_mode = BBS_SCORE_MAX;
+  p->error_move = BBS_ERROR_BETA_WALK;
+  p->error_step = 1.2f;
 }
 
 int bbs_pruefer_to_parent_vector(const uint32_t *code, uint32_t code_len,
@@ -479,26 +560,13 @@ int bbs_create(bbs_ctx **out, const uint64_t *is_mutated,
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, c->device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    // Cell rows: genes only (bits >= n_genes cleared), mutated within known.
-    std::vector<uint64_t> K((size_t)n_cells * c->W64), M(K.size());
-    int64_t sum_k = 0, sum_m = 0;
-    for (uint32_t cell = 0; cell < n_cells; cell++)
-      for (uint32_t k = 0; k < c->W64; k++) {
-        uint64_t mask = ~0ull;
-        const uint32_t lo = 64 * k;
-        if (lo >= n_genes) mask = 0;
-        else if (n_genes - lo < 64) mask = (1ull << (n_genes - lo)) - 1ull;
-        const size_t i = (size_t)cell * c->W64 + k;
-        K[i] = is_known[i] & mask;
-        M[i] = is_mutated[i] & K[i];
-        sum_k += __builtin_popcountll(K[i]);
-        sum_m += __builtin_popcountll(M[i]);
-      }
-    const size_t bytes = sizeof(uint64_t) * K.size();
+    HostDataset h;
+    prepare_dataset(params, n_cells, n_genes, is_mutated, is_known, h);
+    const size_t bytes = sizeof(uint64_t) * h.K.size();
     if (e == cudaSuccess) e = cudaMalloc(&c->d_K, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_M, bytes);
-    if (e == cudaSuccess) e = cudaMemcpy(c->d_K, K.data(), bytes, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(c->d_M, M.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_K, h.K.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_M, h.M.data(), bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
@@ -507,39 +575,22 @@ int bbs_create(bbs_ctx **out, const uint64_t *is_mutated,
       *c->h_cancel = 0;
       e = cudaHostGetDevicePointer((void **)&c->d_cancel, c->h_cancel, 0);
     }
+    h.ds.K = c->d_K;
+    h.ds.M = c->d_M;
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_ds, sizeof(DatasetDev));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_md, sizeof(ModelDev));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_terms, sizeof(h.terms));
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_ds, &h.ds, sizeof(DatasetDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_md, &h.md, sizeof(ModelDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_terms, h.terms, sizeof(h.terms), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       const int rr = cuda_fail((int)e, "bbs_create");
       bbs_destroy(c);
       return rr;
     }
-    // src/TreeScorer.hpp:99-111
-    const float alpha = params->alpha_mean, bm = params->beta_mean, sd = params->beta_sd;
-    DatasetDev &ds = c->ds;
-    ds.K = c->d_K;
-    ds.M = c->d_M;
-    ds.n_cells = (int)n_cells;
-    ds.n_nodes = (int)c->n_nodes;
-    ds.sum_k = (int)sum_k;
-    ds.sum_m = (int)sum_m;
-    ds.l00 = (float)std::log(1.0 - (double)alpha);
-    ds.l10 = logf(alpha);
-    ds.bpa = (float)(((double)(1.0f - bm) * std::pow((double)bm, 2.0) /
-                      std::pow((double)sd, 2.0)) - (double)bm);
-    ds.bpb = ds.bpa * ((1.0f / bm) - 1.0f);
-    ds.lg_ab = logf(tgammaf(ds.bpa + ds.bpb));
-    ds.lg_a = logf(tgammaf(ds.bpa));
-    ds.lg_b = logf(tgammaf(ds.bpb));
-    host_beta_terms(ds, bm, &c->l01_0, &c->l11_0, &c->prior_0);
-    // src/Parameters.hpp:451-584, src/RawMoveDistribution.hpp:119-131
-    const float sum = params->prob_beta_change + params->prob_prune_n_reattach +
-                      params->prob_swap_nodes + params->prob_swap_subtrees;
-    const float pb = params->prob_beta_change / sum;
-    const float pp = params->prob_prune_n_reattach / sum;
-    const float ps = params->prob_swap_nodes / sum;
-    c->mp.cum_beta = pb;
-    c->mp.cum_prune = pb + pp;
-    c->mp.cum_swap = pb + pp + ps;
-    c->mp.beta_jump_sd = sd / params->beta_jump_scaling_chi;
+    c->ds = h.ds;
+    c->md = h.md;
+    std::memcpy(c->terms, h.terms, sizeof(h.terms));
     c->q = pick_q((int)n_cells);
     *out = c;
     return BBS_OK;
@@ -554,6 +605,9 @@ void bbs_destroy(bbs_ctx *c) {
   free_chains(c);
   cudaFree(c->d_K);
   cudaFree(c->d_M);
+  cudaFree(c->d_ds);
+  cudaFree(c->d_md);
+  cudaFree(c->d_terms);
   cudaFree(c->d_status);
   if (c->h_cancel) cudaFreeHost(c->h_cancel);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -675,9 +729,20 @@ int bbs_init_chains(bbs_ctx *c, uint32_t n_chains, const uint32_t *parents) {
       return cuda_fail((int)e, "bbs_init_chains");
     }
     c->n_chains = n_chains;
-    std::vector<float> betas(n_chains, c->params.beta_mean);
-    const int r = score_device(c, c->d_rows, betas.data(), n_chains, nullptr,
-                               nullptr, nullptr, c->d_states);
+    InitArgs ia{};
+    ia.ds = c->d_ds;
+    ia.md = c->d_md;
+    ia.chain_ds = nullptr;
+    ia.chain_off = nullptr;
+    ia.terms = c->d_terms;
+    ia.n_chains = (int)n_chains;
+    ia.rows = c->d_rows;
+    ia.states = c->d_states;
+    ia.max_nodes = (int)n;
+    const int le = launch_init(ia, w32_of_nodes((int)n),
+                               c->md.score_mode == BBS_SCORE_SUM, c->stream);
+    int r = le != 0 ? cuda_fail(le, "init kernel launch")
+                    : sync_stream(c, "init kernel");
     if (r != BBS_OK) free_chains(c);
     default_launch(c);
     return r;
@@ -692,11 +757,9 @@ int start_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *d_moves,
               bbs_step_trace *d_trace) {
   RunArgs a{};
   a.ds = c->ds;
-  a.mp = c->mp;
-  a.gamma = c->params.gamma;
+  a.md = c->md;
   a.n_chains = (int)c->n_chains;
   a.n_steps = (int)n_steps;
-  a.seed = c->params.seed;
   a.rows = c->d_rows;
   a.best_rows = c->d_best;
   a.states = c->d_states;
@@ -926,8 +989,8 @@ int bbs_get_best(bbs_ctx *c, uint64_t *am, uint64_t *dm, uint32_t *parent,
   }
 }
 
-int bbs_get_chains(bbs_ctx *c, uint64_t *dm, float *beta, float *score,
-                   uint64_t *counts) {
+int bbs_get_chains(bbs_ctx *c, uint64_t *dm, float *alpha, float *beta,
+                   float *score, uint64_t *counts, uint32_t *err_stats) {
   try {
     if (!c) return fail(BBS_ERR_INPUT, "NULL context");
     if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
@@ -940,6 +1003,7 @@ int bbs_get_chains(bbs_ctx *c, uint64_t *dm, float *beta, float *score,
     BBS_CUDA(cudaMemcpy(st.data(), c->d_states, sizeof(ChainState) * st.size(),
                         cudaMemcpyDeviceToHost), "state copy");
     for (uint32_t i = 0; i < c->n_chains; i++) {
+      if (alpha) alpha[i] = st[i].alpha;
       if (beta) beta[i] = st[i].beta;
       if (score) score[i] = st[i].score;
       if (counts) {
@@ -949,11 +1013,28 @@ int bbs_get_chains(bbs_ctx *c, uint64_t *dm, float *beta, float *score,
         counts[4 * i + 2] = (uint64_t)(c->ds.sum_m - sm);
         counts[4 * i + 3] = (uint64_t)sm;
       }
+      if (err_stats) {
+        err_stats[2 * i] = st[i].err_proposed;
+        err_stats[2 * i + 1] = st[i].err_accepted;
+      }
     }
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_get_chains");
   }
+}
+
+int bbs_get_best_alpha(bbs_ctx *c, float *alpha) {
+  if (!c || !alpha) return fail(BBS_ERR_INPUT, "NULL argument");
+  uint32_t chain = 0;
+  const int r = bbs_get_best(c, nullptr, nullptr, nullptr, nullptr, nullptr,
+                             nullptr, &chain);
+  if (r != BBS_OK) return r;
+  ChainState st;
+  BBS_CUDA(cudaMemcpy(&st, c->d_states + chain, sizeof(ChainState),
+                      cudaMemcpyDeviceToHost), "state copy");
+  *alpha = st.best_alpha;
+  return BBS_OK;
 }
 
 int bbs_score_trees(bbs_ctx *c, const uint64_t *dm, const float *betas,
@@ -1231,3 +1312,490 @@ extern "C" int bbs_score_trees_noalloc(bbs_ctx *c, const uint64_t *dm_device,
   return sync_stream(c, "score kernel");
 }
 
+
+// ------------------------------------------------------------------------
+// Many datasets in one launch
+// ------------------------------------------------------------------------
+struct bbs_batch {
+  int device = 0, n_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> side;  // one per launch group (graph branches)
+  std::vector<cudaEvent_t> side_ev;
+  cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
+  uint32_t n_datasets = 0;
+  std::vector<uint32_t> n_cells, n_genes;
+  std::vector<DatasetDev> ds;
+  std::vector<ModelDev> md;
+  std::vector<float> terms;  // [n_datasets][8]
+  bool sum = false;
+  uint32_t *d_cells = nullptr;
+  DatasetDev *d_ds = nullptr;
+  ModelDev *d_md = nullptr;
+  float *d_terms = nullptr;
+  // chains
+  uint32_t cpd = 0, n_chains = 0;
+  std::vector<uint32_t> chain_ds;
+  std::vector<uint64_t> chain_off;
+  size_t row_words = 0;
+  uint32_t *d_rows = nullptr, *d_best = nullptr;
+  ChainState *d_states = nullptr;
+  uint32_t *d_chain_ds = nullptr;
+  uint64_t *d_chain_off = nullptr;
+  // launch groups (row width), rebuilt when the shape changes
+  struct Group {
+    int w32 = 0, max_nodes = 0;
+    std::vector<uint32_t> units;
+    uint32_t *d_units = nullptr;
+  };
+  std::vector<Group> groups;
+  unsigned int *d_counters = nullptr;
+  int *d_status = nullptr;
+  int q = 2, wpb = 4, merge = 0;
+  // graph of the current shape and step count
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_steps = 0;
+  float last_ms = 0.0f;
+};
+
+namespace {
+
+void batch_free_groups(bbs_batch *b) {
+  for (auto &g : b->groups) cudaFree(g.d_units);
+  b->groups.clear();
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_steps = 0;
+}
+
+void batch_free_chains(bbs_batch *b) {
+  batch_free_groups(b);
+  cudaFree(b->d_rows);
+  cudaFree(b->d_best);
+  cudaFree(b->d_states);
+  cudaFree(b->d_chain_ds);
+  cudaFree(b->d_chain_off);
+  b->d_rows = b->d_best = nullptr;
+  b->d_states = nullptr;
+  b->d_chain_ds = nullptr;
+  b->d_chain_off = nullptr;
+  b->n_chains = 0;
+}
+
+// Launch groups for the current shape: one per row width (exact, or the
+// even width of its row stride with merge), chains costliest first.
+int batch_build_groups(bbs_batch *b) {
+  batch_free_groups(b);
+  std::vector<int> key(b->n_datasets);
+  for (uint32_t d = 0; d < b->n_datasets; d++) {
+    int w = w32_of_nodes((int)b->n_genes[d] + 1);
+    if (b->merge) w = rs_of_w32(w);
+    key[d] = w;
+  }
+  for (int w = 1; w <= kMaxW32; w++) {
+    bbs_batch::Group g;
+    g.w32 = w;
+    std::vector<std::pair<double, uint32_t>> cost;
+    for (uint32_t c = 0; c < b->n_chains; c++) {
+      const uint32_t d = b->chain_ds[c];
+      if (key[d] != w) continue;
+      const double groups = (b->n_cells[d] + 31) / 32;
+      const double nodes = b->n_genes[d] + 1.0;
+      cost.push_back({groups * nodes * w + 4.0 * nodes, c});
+      g.max_nodes = std::max(g.max_nodes, (int)nodes);
+    }
+    if (cost.empty()) continue;
+    std::stable_sort(cost.begin(), cost.end(),
+                     [](const auto &x, const auto &y) { return x.first > y.first; });
+    for (auto &p : cost) g.units.push_back(p.second);
+    BBS_CUDA(cudaMalloc(&g.d_units, sizeof(uint32_t) * g.units.size()), "cudaMalloc");
+    BBS_CUDA(cudaMemcpy(g.d_units, g.units.data(), sizeof(uint32_t) * g.units.size(),
+                        cudaMemcpyHostToDevice), "cudaMemcpy");
+    b->groups.push_back(std::move(g));
+  }
+  while (b->side.size() < b->groups.size()) {
+    cudaStream_t s;
+    cudaEvent_t ev;
+    BBS_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+    BBS_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+    b->side.push_back(s);
+    b->side_ev.push_back(ev);
+  }
+  return BBS_OK;
+}
+
+// Issues one run: zero the work counters, then one launch per group on its
+// own stream (forked from and joined back into b->stream).
+int batch_issue(bbs_batch *b, uint32_t n_steps) {
+  BBS_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * kMaxW32,
+                           b->stream), "memset");
+  BBS_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(int), b->stream), "memset");
+  BBS_CUDA(cudaEventRecord(b->fork, b->stream), "event");
+  for (size_t g = 0; g < b->groups.size(); g++) {
+    const auto &grp = b->groups[g];
+    BBS_CUDA(cudaStreamWaitEvent(b->side[g], b->fork, 0), "wait");
+    BatchArgs a{};
+    a.ds = b->d_ds;
+    a.md = b->d_md;
+    a.chain_ds = b->d_chain_ds;
+    a.chain_off = b->d_chain_off;
+    a.units = grp.d_units;
+    a.n_units = (int)grp.units.size();
+    a.n_steps = (int)n_steps;
+    a.chains_per_dataset = (int)b->cpd;
+    a.rows = b->d_rows;
+    a.best_rows = b->d_best;
+    a.states = b->d_states;
+    a.next_unit = b->d_counters + g;
+    a.cancel = nullptr;
+    a.status = b->d_status;
+    a.max_nodes = grp.max_nodes;
+    const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;
+    const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
+    if (e != 0) return cuda_fail(e, "batch kernel launch");
+    BBS_CUDA(cudaEventRecord(b->side_ev[g], b->side[g]), "event");
+    BBS_CUDA(cudaStreamWaitEvent(b->stream, b->side_ev[g], 0), "wait");
+  }
+  return BBS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bbs_batch_create(bbs_batch **out, uint32_t n_datasets,
+                     const uint32_t *n_cells, const uint32_t *n_genes,
+                     const uint64_t *const *is_mutated,
+                     const uint64_t *const *is_known,
+                     const bbs_params *params) {
+  try {
+    if (!out || !n_cells || !n_genes || !is_mutated || !is_known || !params)
+      return fail(BBS_ERR_INPUT, "NULL argument to bbs_batch_create");
+    *out = nullptr;
+    if (n_datasets < 1) return fail(BBS_ERR_INPUT, "need at least one dataset");
+    bool sum = false;
+    for (uint32_t d = 0; d < n_datasets; d++) {
+      if (n_genes[d] < 2 || n_genes[d] > BBS_MAX_GENES)
+        return fail(BBS_ERR_SIZE, "dataset %u: gene count %u outside [2, %d]", d,
+                    n_genes[d], BBS_MAX_GENES);
+      if (n_cells[d] < 1 || n_cells[d] > BBS_MAX_CELLS)
+        return fail(BBS_ERR_SIZE, "dataset %u: cell count %u outside [1, %d]", d,
+                    n_cells[d], BBS_MAX_CELLS);
+      if (!is_mutated[d] || !is_known[d])
+        return fail(BBS_ERR_INPUT, "dataset %u: NULL cell rows", d);
+      const int r = check_params(&params[d]);
+      if (r != BBS_OK) return r;
+      if (d > 0 && params[d].score_mode != params[0].score_mode)
+        return fail(BBS_ERR_INPUT, "all datasets of a batch share one score mode");
+      sum = params[d].score_mode == BBS_SCORE_SUM;
+    }
+    int n_dev = 0;
+    if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev < 1)
+      return fail(BBS_ERR_CUDA, "no CUDA device is available");
+    bbs_batch *b = new (std::nothrow) bbs_batch();
+    if (!b) return fail(BBS_ERR_ALLOC, "out of host memory");
+    b->n_datasets = n_datasets;
+    b->n_cells.assign(n_cells, n_cells + n_datasets);
+    b->n_genes.assign(n_genes, n_genes + n_datasets);
+    b->sum = sum;
+    cudaGetDevice(&b->device);
+    cudaDeviceGetAttribute(&b->n_sms, cudaDevAttrMultiProcessorCount, b->device);
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    std::vector<HostDataset> h(n_datasets);
+    size_t words = 0;
+    std::vector<size_t> off(n_datasets);
+    for (uint32_t d = 0; d < n_datasets; d++) {
+      prepare_dataset(&params[d], n_cells[d], n_genes[d], is_mutated[d],
+                      is_known[d], h[d]);
+      off[d] = words;
+      words += 2 * h[d].K.size();  // uint32 words of K, then of M
+      words = (words + 7) & ~(size_t)7;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_cells, sizeof(uint32_t) * 2 * std::max<size_t>(words, 1));
+    b->ds.resize(n_datasets);
+    b->md.resize(n_datasets);
+    b->terms.resize(8 * (size_t)n_datasets);
+    for (uint32_t d = 0; d < n_datasets && e == cudaSuccess; d++) {
+      uint32_t *base = b->d_cells + 2 * off[d];
+      const size_t kw = 2 * h[d].K.size();  // uint32 words of K
+      e = cudaMemcpy(base, h[d].K.data(), sizeof(uint32_t) * kw, cudaMemcpyHostToDevice);
+      if (e == cudaSuccess)
+        e = cudaMemcpy(base + kw, h[d].M.data(), sizeof(uint32_t) * kw,
+                       cudaMemcpyHostToDevice);
+      h[d].ds.K = base;
+      h[d].ds.M = base + kw;
+      b->ds[d] = h[d].ds;
+      b->md[d] = h[d].md;
+      std::memcpy(&b->terms[8 * d], h[d].terms, sizeof(h[d].terms));
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_ds, sizeof(DatasetDev) * n_datasets);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_md, sizeof(ModelDev) * n_datasets);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_terms, sizeof(float) * b->terms.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_ds, b->ds.data(), sizeof(DatasetDev) * n_datasets,
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_md, b->md.data(), sizeof(ModelDev) * n_datasets,
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_terms, b->terms.data(), sizeof(float) * b->terms.size(),
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_counters, sizeof(unsigned int) * kMaxW32);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int));
+    if (e != cudaSuccess) {
+      const int r = cuda_fail((int)e, "bbs_batch_create");
+      bbs_batch_destroy(b);
+      return r;
+    }
+    *out = b;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_create");
+  }
+}
+
+void bbs_batch_destroy(bbs_batch *b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  batch_free_chains(b);
+  for (auto s : b->side) cudaStreamDestroy(s);
+  for (auto ev : b->side_ev) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  cudaFree(b->d_cells);
+  cudaFree(b->d_ds);
+  cudaFree(b->d_md);
+  cudaFree(b->d_terms);
+  cudaFree(b->d_counters);
+  cudaFree(b->d_status);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int bbs_batch_init_chains(bbs_batch *b, uint32_t cpd) {
+  try {
+    if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+    if (cpd < 1) return fail(BBS_ERR_INPUT, "need at least one chain per dataset");
+    batch_free_chains(b);
+    const uint32_t n_chains = cpd * b->n_datasets;
+    b->chain_ds.resize(n_chains);
+    b->chain_off.resize(n_chains);
+    size_t words = 0;
+    for (uint32_t d = 0; d < b->n_datasets; d++)
+      for (uint32_t k = 0; k < cpd; k++) {
+        const uint32_t c = d * cpd + k;
+        const uint32_t n = b->n_genes[d] + 1;
+        b->chain_ds[c] = d;
+        b->chain_off[c] = words;
+        words += (size_t)n * 2 * words64(n);
+        words = (words + 7) & ~(size_t)7;  // 32-byte aligned rows
+      }
+    b->row_words = words;
+    std::vector<uint32_t> rows(words, 0u);
+    for (uint32_t d = 0; d < b->n_datasets; d++) {
+      const uint32_t n = b->n_genes[d] + 1;
+      std::vector<uint32_t> pv((size_t)cpd * n);
+      random_parents(b->md[d].seed, b->n_genes[d], cpd, pv.data());
+      std::vector<uint64_t> dm((size_t)n * words64(n));
+      for (uint32_t k = 0; k < cpd; k++) {
+        parent_to_matrix(pv.data() + (size_t)k * n, n, nullptr, dm.data());
+        std::memcpy(rows.data() + b->chain_off[d * cpd + k], dm.data(),
+                    sizeof(uint64_t) * dm.size());
+      }
+    }
+    cudaError_t e = cudaMalloc(&b->d_rows, sizeof(uint32_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_best, sizeof(uint32_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_states, sizeof(ChainState) * n_chains);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_ds, sizeof(uint32_t) * n_chains);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_off, sizeof(uint64_t) * n_chains);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_rows, rows.data(), sizeof(uint32_t) * words,
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->d_best, 0, sizeof(uint32_t) * words);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_chain_ds, b->chain_ds.data(), sizeof(uint32_t) * n_chains,
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_chain_off, b->chain_off.data(), sizeof(uint64_t) * n_chains,
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      batch_free_chains(b);
+      return cuda_fail((int)e, "bbs_batch_init_chains");
+    }
+    b->cpd = cpd;
+    b->n_chains = n_chains;
+    int r = batch_build_groups(b);
+    if (r != BBS_OK) return r;
+    for (const auto &g : b->groups) {
+      InitArgs ia{};
+      ia.ds = b->d_ds;
+      ia.md = b->d_md;
+      ia.chain_ds = b->d_chain_ds;
+      ia.chain_off = b->d_chain_off;
+      ia.terms = b->d_terms;
+      ia.chain_list = g.d_units;
+      ia.n_chains = (int)g.units.size();
+      ia.rows = b->d_rows;
+      ia.states = b->d_states;
+      ia.max_nodes = g.max_nodes;
+      const int le = launch_init(ia, g.w32, b->sum, b->stream);
+      if (le != 0) return cuda_fail(le, "init kernel launch");
+    }
+    BBS_CUDA(cudaStreamSynchronize(b->stream), "init kernel");
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_init_chains");
+  }
+}
+
+int bbs_batch_run(bbs_batch *b, uint32_t n_steps) {
+  if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+  if (b->n_chains == 0) return fail(BBS_ERR_STATE, "bbs_batch_init_chains was not called");
+  if (n_steps == 0) return BBS_OK;
+  if (n_steps > 0x7fffffffu) return fail(BBS_ERR_SIZE, "too many steps");
+  if (b->graph == nullptr || b->graph_steps != n_steps) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    BBS_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal),
+             "begin capture");
+    const int r = batch_issue(b, n_steps);
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (r != BBS_OK) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    BBS_CUDA(ce, "end capture");
+    const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    BBS_CUDA(ie, "graph instantiate");
+    b->graph_steps = n_steps;
+  }
+  BBS_CUDA(cudaEventRecord(b->ev0, b->stream), "event");
+  BBS_CUDA(cudaGraphLaunch(b->graph, b->stream), "graph launch");
+  BBS_CUDA(cudaEventRecord(b->ev1, b->stream), "event");
+  BBS_CUDA(cudaStreamSynchronize(b->stream), "batch run");
+  BBS_CUDA(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "event timing");
+  return BBS_OK;
+}
+
+int bbs_batch_last_run_ms(const bbs_batch *b, float *ms) {
+  if (!b || !ms) return fail(BBS_ERR_INPUT, "NULL argument");
+  *ms = b->last_ms;
+  return BBS_OK;
+}
+
+int bbs_batch_set_launch(bbs_batch *b, int q, int wpb, int merge) {
+  if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+  if (q != 0 && q != 1 && q != 2 && q != 4)
+    return fail(BBS_ERR_INPUT, "cells per lane must be 1, 2 or 4");
+  if (wpb < 0 || wpb > 4) return fail(BBS_ERR_INPUT, "warps per block must be in [1, 4]");
+  if (q) b->q = q;
+  if (wpb) b->wpb = wpb;
+  if (merge >= 0 && merge != b->merge) {
+    b->merge = merge ? 1 : 0;
+    if (b->n_chains) {
+      const int r = batch_build_groups(b);
+      if (r != BBS_OK) return r;
+    }
+  }
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  return BBS_OK;
+}
+
+int bbs_batch_get_launch(const bbs_batch *b, int *q, int *wpb, int *merge) {
+  if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+  if (q) *q = b->q;
+  if (wpb) *wpb = b->wpb;
+  if (merge) *merge = b->merge;
+  return BBS_OK;
+}
+
+int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
+  try {
+    if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+    if (b->n_chains == 0) return fail(BBS_ERR_STATE, "bbs_batch_init_chains was not called");
+    if (probe_steps == 0) probe_steps = 64;
+    const size_t rb = sizeof(uint32_t) * b->row_words;
+    const size_t sb = sizeof(ChainState) * b->n_chains;
+    DevBuf<uint8_t> sr, sbst, sst;
+    BBS_CUDA(sr.alloc(rb), "cudaMalloc");
+    BBS_CUDA(sbst.alloc(rb), "cudaMalloc");
+    BBS_CUDA(sst.alloc(sb), "cudaMalloc");
+    auto cp = [&](void *d, const void *s, size_t n) {
+      return cudaMemcpyAsync(d, s, n, cudaMemcpyDeviceToDevice, b->stream);
+    };
+    BBS_CUDA(cp(sr.p, b->d_rows, rb), "save");
+    BBS_CUDA(cp(sbst.p, b->d_best, rb), "save");
+    BBS_CUDA(cp(sst.p, b->d_states, sb), "save");
+    float best = 1e30f;
+    int bq = b->q, bw = b->wpb, bm = b->merge;
+    for (int merge : {0, 1})
+      for (int q : {1, 2, 4})
+        for (int wpb : {1, 2, 4}) {
+          int r = bbs_batch_set_launch(b, q, wpb, merge);
+          if (r != BBS_OK) return r;
+          BBS_CUDA(cudaEventRecord(b->ev0, b->stream), "event");
+          r = batch_issue(b, probe_steps);
+          if (r != BBS_OK) return r;
+          BBS_CUDA(cudaEventRecord(b->ev1, b->stream), "event");
+          BBS_CUDA(cudaStreamSynchronize(b->stream), "probe");
+          float ms = 0;
+          BBS_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1), "timing");
+          if (ms < best) {
+            best = ms;
+            bq = q;
+            bw = wpb;
+            bm = merge;
+          }
+          BBS_CUDA(cp(b->d_rows, sr.p, rb), "restore");
+          BBS_CUDA(cp(b->d_best, sbst.p, rb), "restore");
+          BBS_CUDA(cp(b->d_states, sst.p, sb), "restore");
+        }
+    const int r = bbs_batch_set_launch(b, bq, bw, bm);
+    BBS_CUDA(cudaStreamSynchronize(b->stream), "restore");
+    if (best_ms) *best_ms = best;
+    return r;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_autotune");
+  }
+}
+
+int bbs_batch_get_best(bbs_batch *b, uint32_t dataset, uint64_t *dm,
+                       uint32_t *parent, float *alpha, float *beta,
+                       float *score) {
+  try {
+    if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+    if (b->n_chains == 0) return fail(BBS_ERR_STATE, "no chains");
+    if (dataset >= b->n_datasets) return fail(BBS_ERR_INPUT, "no dataset %u", dataset);
+    std::vector<ChainState> st(b->cpd);
+    const uint32_t c0 = dataset * b->cpd;
+    BBS_CUDA(cudaMemcpy(st.data(), b->d_states + c0, sizeof(ChainState) * b->cpd,
+                        cudaMemcpyDeviceToHost), "state copy");
+    int best = -1;
+    for (uint32_t k = 0; k < b->cpd; k++) {
+      if (!st[k].has_best) continue;
+      if (best < 0 || st[k].best_score > st[best].best_score) best = (int)k;
+    }
+    if (best < 0) return fail(BBS_ERR_STATE, "no steps have been run");
+    const uint32_t n = b->n_genes[dataset] + 1;
+    std::vector<uint64_t> rows((size_t)n * words64(n));
+    BBS_CUDA(cudaMemcpy(rows.data(), b->d_best + b->chain_off[c0 + best],
+                        sizeof(uint64_t) * rows.size(), cudaMemcpyDeviceToHost),
+             "best copy");
+    if (dm) std::memcpy(dm, rows.data(), sizeof(uint64_t) * rows.size());
+    if (parent) matrix_to_parent(rows.data(), n, parent);
+    if (alpha) *alpha = st[best].best_alpha;
+    if (beta) *beta = st[best].best_beta;
+    if (score) *score = st[best].best_score;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_get_best");
+  }
+}
+
+}  // extern "C"

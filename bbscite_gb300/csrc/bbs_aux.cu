@@ -18,9 +18,47 @@ size_t mcmc_smem_bytes(int n_nodes, int wpc, int cpb) {
 int launch_mcmc(const RunArgs &a, int q, int cpb, int n_sms, void *stream) {
   const int w32 = w32_of_nodes(a.ds.n_nodes);
   cudaStream_t s = (cudaStream_t)stream;
+  const bool sum = a.md.score_mode == 1;
   if (w32 > 4) q = std::min(q, 2);
-  if (w32 <= 4) return launch_mcmc_lo(a, w32, q, cpb, n_sms, s);
-  return launch_mcmc_hi(a, w32, q, cpb, n_sms, s);
+  if (w32 <= 4) return launch_mcmc_lo(a, w32, q, sum, cpb, n_sms, s);
+  return launch_mcmc_hi(a, w32, q, sum, cpb, n_sms, s);
+}
+
+int launch_batch(const BatchArgs &b, int w32, int q, bool sum, int wpb,
+                 int n_sms, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (w32 <= 4) return launch_batch_lo(b, w32, q, sum, wpb, n_sms, s);
+  return launch_batch_hi(b, w32, q, sum, wpb, n_sms, s);
+}
+
+template <int W32, bool SUM>
+static int launch_init_t(const InitArgs &a, cudaStream_t s) {
+  constexpr int RS = rs_of_w32(W32), WPB = 4, Q = 2;
+  const size_t smem = (size_t)WPB * a.max_nodes * RS * sizeof(uint32_t);
+  auto kern = init_kernel<W32, Q, SUM>;
+  cudaError_t e = prepare_smem(kern, smem);
+  if (e != cudaSuccess) return (int)e;
+  kern<<<(a.n_chains + WPB - 1) / WPB, WPB * 32, smem, s>>>(a);
+  return (int)cudaGetLastError();
+}
+
+int launch_init(const InitArgs &a, int w32, bool sum, void *stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (w32 * 2 + (sum ? 1 : 0)) {
+#define BBS_INIT_CASE(W)                          \
+  case W * 2: return launch_init_t<W, false>(a, s); \
+  case W * 2 + 1: return launch_init_t<W, true>(a, s);
+    BBS_INIT_CASE(1)
+    BBS_INIT_CASE(2)
+    BBS_INIT_CASE(3)
+    BBS_INIT_CASE(4)
+    BBS_INIT_CASE(5)
+    BBS_INIT_CASE(6)
+    BBS_INIT_CASE(7)
+    BBS_INIT_CASE(8)
+#undef BBS_INIT_CASE
+    default: return (int)cudaErrorInvalidValue;
+  }
 }
 
 template <int W32, bool ATTACH>

@@ -528,30 +528,119 @@ __device__ __forceinline__ void counts_at(const uint32_t *rows,
   }
 }
 
-// This warp's part of the class sums over its cells.  Cells are split over
-// the `wpc` warps of a chain: cell = c0 + 32*wpc*q + 32*wic + lane.  With
-// `resident`, cb already holds the warp's cells.
+// The log table of one (alpha, beta) state.
+struct LogTable {
+  float l00, l10, l01, l11;
+};
+
+// This warp's part of the class sums over its cells (max score).  Cells
+// are split over the `wpc` warps of a chain: cell = c0 + 32*wpc*q +
+// 32*wic + lane.  With `resident`, cb already holds the warp's cells.
 template <int W32, int Q>
 __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
                                            const DatasetDev &ds,
                                            Cells<W32, Q> &cb, bool resident,
-                                           float l01, float l11, int wpc,
+                                           const LogTable &L, int wpc,
                                            int wic, int lane, int &sk,
                                            int &sm) {
   int k = 0, m = 0, bj[Q];
   if (resident) {
-    best_nodes<W32, Q>(rows, n, cb, ds.l00, l01, ds.l10, l11, bj);
+    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
     counts_at<W32, Q>(rows, cb, bj, k, m);
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      best_nodes<W32, Q>(rows, n, cb, ds.l00, l01, ds.l10, l11, bj);
+      best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
       counts_at<W32, Q>(rows, cb, bj, k, m);
     }
   }
   sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);
   sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
+}
+
+// Sum-over-attachments pass with its adjoint, for the lane's Q cells:
+// per cell an online logsumexp over nodes carries the softmax-weighted
+// sums of d = popc(D & A) and m = popc(M & A).  Adds to acc[5], in fixed
+// point (2^-20 units, so the result does not depend on how cells are
+// split over lanes and warps): sum_c lse_c and the expected class counts
+// E[n00], E[n01], E[n10], E[n11].
+inline constexpr float kFixScale = 1048576.0f;  // 2^20
+
+template <int W32, int Q>
+__device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
+                                          const Cells<W32, Q> &cb,
+                                          const LogTable &L, int c0, int stride,
+                                          int lane, int n_cells,
+                                          long long (&acc)[5]) {
+  constexpr int RS = rs_of_w32(W32);
+  float mx[Q], z[Q], ed[Q], em[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    mx[q] = -INFINITY;
+    z[q] = ed[q] = em[q] = 0.0f;
+  }
+#pragma unroll 1
+  for (int j = 0; j < n; j++) {
+    uint32_t a[W32];
+    ld_row<W32>(rows + j * RS, a);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const int d = masked_popc<W32>(cb.D[q], a);
+      const int m = masked_popc<W32>(cb.M[q], a);
+      const float s = pair_score(d, m, cb.pdb[q], cb.pmb[q], L.l00, L.l01,
+                                 L.l10, L.l11);
+      const float fd = __fsub_rn(__int_as_float(0x4B000000 + d), 8388608.0f);
+      const float fm = __fsub_rn(__int_as_float(0x4B000000 + m), 8388608.0f);
+      const float dl = s - mx[q];
+      const bool up = dl > 0.0f;  // new running maximum
+      const float e = __expf(-fabsf(dl));
+      z[q] = up ? fmaf(z[q], e, 1.0f) : z[q] + e;
+      ed[q] = up ? fmaf(ed[q], e, fd) : fmaf(e, fd, ed[q]);
+      em[q] = up ? fmaf(em[q], e, fm) : fmaf(e, fm, em[q]);
+      mx[q] = up ? s : mx[q];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int c = c0 + stride * q + lane;
+    if (c >= n_cells) continue;
+    const float inv = 1.0f / z[q];
+    const float Ed = ed[q] * inv, Em = em[q] * inv;
+    const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
+    acc[0] += __float2ll_rn((mx[q] + logf(z[q])) * kFixScale);
+    acc[1] += __float2ll_rn((pd - Ed) * kFixScale);  // E[n00]
+    acc[2] += __float2ll_rn(Ed * kFixScale);         // E[n01]
+    acc[3] += __float2ll_rn((pm - Em) * kFixScale);  // E[n10]
+    acc[4] += __float2ll_rn(Em * kFixScale);         // E[n11]
+  }
+}
+
+// This warp's part of the sum score and expected counts (fixed point,
+// warp-reduced).
+template <int W32, int Q>
+__device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
+                                         const DatasetDev &ds,
+                                         Cells<W32, Q> &cb, bool resident,
+                                         const LogTable &L, int wpc, int wic,
+                                         int lane, long long (&acc)[5]) {
+#pragma unroll
+  for (int i = 0; i < 5; i++) acc[i] = 0;
+  if (resident) {
+    sum_cells<W32, Q>(rows, n, cb, L, 32 * wic, 32 * wpc, lane, ds.n_cells,
+                      acc);
+  } else {
+    const int span = 32 * wpc * Q;
+    for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
+      load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
+      sum_cells<W32, Q>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc, lane,
+                        ds.n_cells, acc);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+    for (int i = 0; i < 5; i++) acc[i] += __shfl_xor_sync(BBS_FULL_MASK, acc[i], off);
 }
 
 // Class totals (n00, n01, n10, n11) from the sums.
@@ -565,14 +654,14 @@ __device__ __forceinline__ void class_totals(const DatasetDev &ds, int sk,
 
 // ((l00*N00 + l01*N01) + l10*N10) + l11*N11 + prior, no contraction.
 __device__ __forceinline__ float tree_score(const DatasetDev &ds, int sk,
-                                           int sm, float l01, float l11,
+                                           int sm, const LogTable &L,
                                            float prior) {
   int N[4];
   class_totals(ds, sk, sm, N);
-  float t = __fmul_rn((float)N[0], ds.l00);
-  t = __fadd_rn(t, __fmul_rn((float)N[1], l01));
-  t = __fadd_rn(t, __fmul_rn((float)N[2], ds.l10));
-  t = __fadd_rn(t, __fmul_rn((float)N[3], l11));
+  float t = __fmul_rn((float)N[0], L.l00);
+  t = __fadd_rn(t, __fmul_rn((float)N[1], L.l01));
+  t = __fadd_rn(t, __fmul_rn((float)N[2], L.l10));
+  t = __fadd_rn(t, __fmul_rn((float)N[3], L.l11));
   return __fadd_rn(t, prior);
 }
 
@@ -587,6 +676,70 @@ __device__ __forceinline__ void beta_terms(const DatasetDev &ds, float beta,
   r = __fadd_rn(r, __fmul_rn(__fsub_rn(ds.bpb, 1.0f), logf(__fsub_rn(1.0f, beta))));
   r = __fsub_rn(r, ds.lg_a);
   prior = __fsub_rn(r, ds.lg_b);
+}
+
+// The alpha-dependent entries, as the reference's ctor computes them.
+__device__ __forceinline__ void alpha_terms(float alpha, float &l00,
+                                            float &l10) {
+  l00 = (float)log(1.0 - (double)alpha);
+  l10 = logf(alpha);
+}
+
+// ------------------------------------------------------------------------
+// Error-rate moves in (a, b) = (logit alpha, logit beta).  The target is
+//   gamma * S(alpha, beta) + log(alpha (1-alpha)) + log(beta (1-beta)),
+// S = data term + log Beta prior(beta), the Jacobian terms making it the
+// density of (a, b).  Expected (or, for the max score, exact) class counts
+// e[4] = (n00, n01, n10, n11) give the gradient and a diagonal
+// preconditioner M = 1 / (1 + curvature) from the same counts.
+// ------------------------------------------------------------------------
+struct ErrorGeom {
+  float grad_a, grad_b, prec_a, prec_b;
+};
+
+__device__ __forceinline__ ErrorGeom error_geometry(const DatasetDev &ds,
+                                                    float alpha, float beta,
+                                                    float gamma,
+                                                    const float (&e)[4]) {
+  ErrorGeom g;
+  const float va = alpha * (1.0f - alpha), vb = beta * (1.0f - beta);
+  const float dS_da = -e[0] / (1.0f - alpha) + e[2] / alpha;
+  const float dS_db = e[1] / beta - e[3] / (1.0f - beta) +
+                      (ds.bpa - 1.0f) / beta - (ds.bpb - 1.0f) / (1.0f - beta);
+  g.grad_a = gamma * va * dS_da + (1.0f - 2.0f * alpha);
+  g.grad_b = gamma * vb * dS_db + (1.0f - 2.0f * beta);
+  g.prec_a = 1.0f / (1.0f + gamma * (e[0] + e[2]) * va);
+  g.prec_b = 1.0f / (1.0f + gamma * (e[1] + e[3] + fmaxf(ds.bpa + ds.bpb - 2.0f, 0.0f)) * vb);
+  return g;
+}
+
+__device__ __forceinline__ float logit(float p) { return logf(p) - log1pf(-p); }
+__device__ __forceinline__ float sigmoid(float x) { return 1.0f / (1.0f + __expf(-x)); }
+
+// log q(to | from) of the (preconditioned, optionally gradient-drifted)
+// Gaussian proposal, up to the constant shared by both directions.
+__device__ __forceinline__ float log_q(float ta, float tb, float fa, float fb,
+                                       const ErrorGeom &g, float eps,
+                                       bool drift) {
+  const float h = drift ? 0.5f * eps * eps : 0.0f;
+  const float ra = ta - fa - h * g.prec_a * g.grad_a;
+  const float rb = tb - fb - h * g.prec_b * g.grad_b;
+  const float e2 = eps * eps;
+  return -(ra * ra) / (2.0f * e2 * g.prec_a) - (rb * rb) / (2.0f * e2 * g.prec_b) -
+         0.5f * (logf(g.prec_a) + logf(g.prec_b));
+}
+
+// Two standard normals from the move's two uniforms (Box-Muller); the
+// record's raw_descendant_of_v / raw_nondescendant_of_v are unused by
+// error moves, so recorded streams fix these draws too.
+__device__ __forceinline__ void error_normals(const bbs_raw_move &raw,
+                                              float &z0, float &z1) {
+  const float u1 = fmaxf(1.0f - raw.raw_descendant_of_v, 1.0e-30f);
+  const float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * raw.raw_nondescendant_of_v, &s, &c);
+  z0 = r * c;
+  z1 = r * s;
 }
 
 }  // namespace bbs

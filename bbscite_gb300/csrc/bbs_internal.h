@@ -18,7 +18,8 @@ __host__ __device__ constexpr int rs_of_w32(int w32) {
 __host__ __device__ constexpr int w32_of_nodes(int n) { return (n + 31) / 32; }
 
 // Cumulative move thresholds and jump sd (src/RawMoveDistribution.hpp:
-// 119-131, src/Parameters.hpp:451-584).
+// 119-131, src/Parameters.hpp:451-584).  The first threshold is the
+// error-rate move (the reference's ChangeBeta).
 struct MoveProbs {
   float cum_beta, cum_prune, cum_swap, beta_jump_sd;
 };
@@ -29,30 +30,44 @@ struct DatasetDev {
   const uint32_t *M;  // mutated rows [n_cells][RS], pre-masked with K
   int n_cells, n_nodes;
   int sum_k, sum_m;   // sum over cells of popc(K), popc(M)
-  float l00, l10;     // log(1-alpha), log(alpha) (src/TreeScorer.hpp:99-106)
+  float l00, l10;     // log(1-alpha), log(alpha) of alpha_mean
+                      // (src/TreeScorer.hpp:99-106)
   float bpa, bpb;     // Beta prior parameters (src/TreeScorer.hpp:108-111)
   float lg_ab, lg_a, lg_b;  // log(tgamma(a+b)), log(tgamma(a)), log(tgamma(b))
 };
 
-// Persistent per-chain state (64 bytes).
-struct ChainState {
-  float beta, score;
-  float l01, l11, prior;  // log(beta), log(1-beta), logscore_beta(beta)
-  int32_t sk, sm;         // class sums of the current tree
-  uint32_t has_best;
-  float best_beta, best_score;
-  int32_t best_sk, best_sm;
-  uint64_t steps_done;    // Philox step counter
-  uint32_t pad[2];
+// The sampling rules of one dataset's chains.
+struct ModelDev {
+  MoveProbs mp;
+  float gamma;
+  int32_t score_mode;  // 0: max over attachments, 1: sum (logsumexp)
+  int32_t error_move;  // 0: reference beta walk, 1: preconditioned random
+                       // walk on (logit alpha, logit beta), 2: Langevin
+  float error_step;    // step size of error moves 1 and 2
+  uint64_t seed;       // Philox key
 };
-static_assert(sizeof(ChainState) == 64, "ChainState layout");
+
+// Persistent per-chain state (128 bytes).
+struct ChainState {
+  float alpha, beta, score, prior;  // score = data term + log prior(beta)
+  float l00, l10, l01, l11;         // log table of (alpha, beta)
+  float grad_a, grad_b;             // gradient of the error-move target in
+                                    // (logit alpha, logit beta)
+  float prec_a, prec_b;             // diagonal preconditioner there
+  int32_t sk, sm;                   // class sums (max score)
+  uint32_t has_best;
+  float best_alpha, best_beta, best_score;
+  int32_t best_sk, best_sm;
+  uint64_t steps_done;              // Philox step counter
+  uint32_t err_proposed, err_accepted;
+  uint32_t pad[8];
+};
+static_assert(sizeof(ChainState) == 128, "ChainState layout");
 
 struct RunArgs {
   DatasetDev ds;
-  MoveProbs mp;
-  float gamma;
+  ModelDev md;
   int n_chains, n_steps;
-  uint64_t seed;
   uint32_t *rows;       // [n_chains][n_nodes][RS] current trees
   uint32_t *best_rows;  // [n_chains][n_nodes][RS] best proposals
   ChainState *states;
@@ -63,6 +78,40 @@ struct RunArgs {
   int wpc;                    // warps per chain (cells split over them)
 };
 
+// Many datasets in one launch: chains are listed by unit (chain index in
+// an order of decreasing cost); each chain names its dataset and row offset.
+struct BatchArgs {
+  const DatasetDev *ds;      // [n_datasets]
+  const ModelDev *md;        // [n_datasets]
+  const uint32_t *chain_ds;  // [n_chains] dataset of each chain
+  const uint64_t *chain_off; // [n_chains] word offset of its rows
+  const uint32_t *units;     // chains of this launch, costliest first
+  int n_units, n_steps;
+  int chains_per_dataset;    // chain c is number c - d * this of dataset d
+  uint32_t *rows, *best_rows;
+  ChainState *states;
+  unsigned int *next_unit;   // work counter (zeroed before the launch)
+  const volatile int *cancel;
+  int *status;
+  int max_nodes;             // shared memory is sized for this
+};
+
+// Initial state of each chain: evaluate its tree at (alpha_mean,
+// beta_mean) with host-computed log-table terms.
+struct InitArgs {
+  const DatasetDev *ds;      // [n_datasets]
+  const ModelDev *md;
+  const uint32_t *chain_ds;  // null: every chain uses dataset 0
+  const uint64_t *chain_off; // null: chain * n_nodes * RS
+  const float *terms;        // [n_datasets][8]: alpha, beta, l00, l10,
+                             //   l01, l11, prior, unused
+  const uint32_t *chain_list; // null: chains 0..n_chains-1
+  int n_chains;
+  const uint32_t *rows;
+  ChainState *states;
+  int max_nodes;             // shared memory is sized for this
+};
+
 struct ScoreArgs {
   DatasetDev ds;
   const uint32_t *rows;  // [n_trees][n_nodes][RS]
@@ -71,7 +120,7 @@ struct ScoreArgs {
   float *scores;
   uint64_t *counts;      // [n_trees][4] or null
   uint32_t *attach;      // [n_trees][n_cells] or null
-  ChainState *states;    // when set: write score/sk/sm/l01/l11/prior
+  ChainState *states;    // unused (kept zero)
 };
 
 struct ApplyArgs {
@@ -94,10 +143,15 @@ struct GradArgs {
   float *posterior;  // [n_trees][n_cells][n_nodes] or null
 };
 
-// Host launchers (bbs_kernels.cu).  Return a cudaError_t as int.
+// Host launchers (bbs_aux.cu, bbs_mcmc_*.cu).  Return a cudaError_t as int.
 // chains_per_block must be 1 when a.wpc > 1 (the block is one chain).
 int launch_mcmc(const RunArgs &a, int q, int chains_per_block, int n_sms,
                 void *stream);
+int launch_batch(const BatchArgs &b, int w32, int q, bool sum,
+                 int warps_per_block, int n_sms, void *stream);
+// Launch groups: every chain of a launch must store its rows with the
+// stride rs_of_w32(w32) of the launch (w32 at least the chains' own).
+int launch_init(const InitArgs &a, int w32, bool sum, void *stream);
 int launch_score(const ScoreArgs &a, int q, void *stream);
 int launch_apply(const ApplyArgs &a, void *stream);
 int launch_grad(const GradArgs &a, int q, void *stream);

@@ -40,11 +40,253 @@ __device__ __forceinline__ void copy_rows(const uint32_t *src, uint32_t *dst,
   copy_rows_part<W32>(src, dst, n, 1, 0, lane);
 }
 
-// Shared-memory words per chain slot: two row buffers, the partial class
-// sums of both step parities (2 x wpc x 2 ints) and a flag word, padded to
+// Shared-memory words per chain slot: two row buffers, the partial sums
+// of both step parities (2 x wpc x 12 words) and a flag word, padded to
 // 16 bytes.
 __host__ __device__ inline int slot_words(int n, int rs, int wpc) {
-  return 2 * n * rs + 4 * wpc + 4;
+  return 2 * n * rs + 24 * wpc + 4;
+}
+
+// Evaluates a tree for the whole chain (all wpc warps): returns the score
+// S = data term + prior and the (exact or expected) class counts e[4];
+// sk, sm are the class sums of the max score.
+template <int W32, int Q, bool SUM>
+__device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
+                                          const DatasetDev &ds,
+                                          Cells<W32, Q> &cb, bool resident,
+                                          const LogTable &L, float prior,
+                                          int wpc, int wic, int lane,
+                                          int *part, int parity,
+                                          float (&e)[4], int &sk, int &sm) {
+  if constexpr (!SUM) {
+    int a, b;
+    score_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, a, b);
+    if (wpc > 1) {
+      int *pp = part + parity * 12 * wpc;
+      if (lane == 0) {
+        pp[12 * wic] = a;
+        pp[12 * wic + 1] = b;
+      }
+      __syncthreads();
+      a = b = 0;
+      for (int w = 0; w < wpc; w++) {
+        a += pp[12 * w];
+        b += pp[12 * w + 1];
+      }
+    }
+    sk = a;
+    sm = b;
+    int N[4];
+    class_totals(ds, sk, sm, N);
+#pragma unroll
+    for (int i = 0; i < 4; i++) e[i] = (float)N[i];
+    return tree_score(ds, sk, sm, L, prior);
+  } else {
+    long long acc[5];
+    sum_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, acc);
+    if (wpc > 1) {
+      long long *pp = reinterpret_cast<long long *>(part) + parity * 6 * wpc;
+      if (lane == 0)
+        for (int i = 0; i < 5; i++) pp[6 * wic + i] = acc[i];
+      __syncthreads();
+      for (int i = 0; i < 5; i++) acc[i] = 0;
+      for (int w = 0; w < wpc; w++)
+        for (int i = 0; i < 5; i++) acc[i] += pp[6 * w + i];
+    }
+    sk = sm = 0;
+#pragma unroll
+    for (int i = 0; i < 4; i++) e[i] = (float)((double)acc[i + 1] / kFixScale);
+    return __fadd_rn((float)((double)acc[0] / kFixScale), prior);
+  }
+}
+
+// One chain for n_steps steps: src/Application.hpp:408-487 with the
+// error-rate move chosen by md.error_move.  `chain_id` keys the Philox
+// stream.  All wpc warps of the chain run this with the same arguments.
+template <int W32, int Q, bool SUM>
+__device__ __forceinline__ void run_chain(
+    const DatasetDev &ds, const ModelDev &md, uint32_t chain_id,
+    uint32_t *g, uint32_t *gbest, ChainState *gstate,
+    const bbs_raw_move *moves, bbs_step_trace *trace, int n_steps,
+    const volatile int *cancel, int *status, uint32_t *buf0, uint32_t *buf1,
+    int *part, volatile int *sflag, Cells<W32, Q> &cb, bool resident, int wpc,
+    int wic, int lane) {
+  const int n = ds.n_nodes;
+  const bool multi = wpc > 1;
+  const ChainState st = *gstate;
+  copy_rows_part<W32>(g, buf0, n, wpc, wic, lane);
+  if (multi) __syncthreads(); else __syncwarp();
+  uint32_t *cur = buf0, *prop = buf1;
+  float alpha = st.alpha, beta = st.beta, score = st.score, prior = st.prior;
+  LogTable L{st.l00, st.l10, st.l01, st.l11};
+  ErrorGeom geo{st.grad_a, st.grad_b, st.prec_a, st.prec_b};
+  int csk = st.sk, csm = st.sm;
+  bool has_best = st.has_best != 0;
+  float best_score = st.best_score, best_alpha = st.best_alpha,
+        best_beta = st.best_beta;
+  int bsk = st.best_sk, bsm = st.best_sm;
+  uint32_t err_prop = st.err_proposed, err_acc = st.err_accepted;
+  const bool learn = md.error_move != 0;
+  int i = 0;
+  bool cancelled = false;
+  for (; i < n_steps; i++) {
+    if (cancel != nullptr && (i & 255) == 0) {
+      // one reader, then a chain-uniform decision
+      if (wic == 0 && lane == 0) *sflag = *cancel;
+      if (multi) __syncthreads(); else __syncwarp();
+      const int c = *sflag;
+      if (multi) __syncthreads(); else __syncwarp();
+      if (c) {
+        cancelled = true;
+        break;
+      }
+    }
+    const uint64_t step = st.steps_done + (uint64_t)i;
+    const bbs_raw_move raw =
+        moves != nullptr ? moves[i]
+                         : sample_move(md.mp, (uint32_t)n, md.seed, chain_id,
+                                       step, trace != nullptr);
+    const bool err_move = raw.move_type == BBS_MOVE_CHANGE_BETA;
+    float palpha = alpha, pbeta = beta, pprior = prior;
+    LogTable PL = L;
+    const uint32_t *scored = cur;
+    float corr = 1.0f;
+    float fa = 0.0f, fb = 0.0f, ta = 0.0f, tb = 0.0f;
+    uint32_t Dv[W32], Dw[W32];
+    if (!err_move) {
+      const Realized R = realize_move<W32>(cur, n, beta, raw, lane, Dv, Dw);
+      build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
+                          lane);
+      scored = prop;
+      // src/Application.hpp:443-450
+      if (raw.move_type == BBS_MOVE_SWAP_SUBTREES && R.related)
+        corr = __fdiv_rn((float)R.ndv, (float)R.ndw);
+    } else if (!learn) {
+      // reference ChangeBeta: beta + jump reflected into [0, 1]
+      // (src/MutationTree.hpp:345-351)
+      float nb = __fadd_rn(beta, raw.beta_jump);
+      if (nb < 0.0f) nb = fabsf(nb);
+      if (nb > 1.0f) nb = __fsub_rn(nb, __fmul_rn(2.0f, __fsub_rn(nb, 1.0f)));
+      pbeta = nb;
+      beta_terms(ds, pbeta, PL.l01, PL.l11, pprior);
+    } else {
+      // (preconditioned) random walk or Langevin step in logit space
+      float z0, z1;
+      error_normals(raw, z0, z1);
+      const float eps = md.error_step;
+      const float h = md.error_move == 2 ? 0.5f * eps * eps : 0.0f;
+      fa = logit(alpha);
+      fb = logit(beta);
+      ta = fa + h * geo.prec_a * geo.grad_a + eps * sqrtf(geo.prec_a) * z0;
+      tb = fb + h * geo.prec_b * geo.grad_b + eps * sqrtf(geo.prec_b) * z1;
+      palpha = fminf(fmaxf(sigmoid(ta), 1.0e-7f), 1.0f - 1.0e-7f);
+      pbeta = fminf(fmaxf(sigmoid(tb), 1.0e-7f), 1.0f - 1.0e-7f);
+      ta = logit(palpha);
+      tb = logit(pbeta);
+      alpha_terms(palpha, PL.l00, PL.l10);
+      beta_terms(ds, pbeta, PL.l01, PL.l11, pprior);
+    }
+    if (multi) __syncthreads(); else __syncwarp();
+    float e[4];
+    int sk, sm;
+    const float pscore = evaluate<W32, Q, SUM>(scored, n, ds, cb, resident, PL,
+                                               pprior, wpc, wic, lane, part,
+                                               i & 1, e, sk, sm);
+    ErrorGeom pgeo = geo;
+    if (learn) pgeo = error_geometry(ds, palpha, pbeta, md.gamma, e);
+    bool accept;
+    if (err_move && learn) {
+      const float logj = logf(alpha * (1.0f - alpha)) + logf(beta * (1.0f - beta));
+      const float plogj =
+          logf(palpha * (1.0f - palpha)) + logf(pbeta * (1.0f - pbeta));
+      const bool drift = md.error_move == 2;
+      const float logr = md.gamma * (pscore - score) + plogj - logj +
+                         log_q(fa, fb, ta, tb, pgeo, md.error_step, drift) -
+                         log_q(ta, tb, fa, fb, geo, md.error_step, drift);
+      accept = logr > logf(raw.acceptance_level);
+      err_prop++;
+      if (accept) err_acc++;
+    } else {
+      // src/Application.hpp:452-455
+      const float ratio = __fmul_rn(
+          corr, expf(__fmul_rn(__fsub_rn(pscore, score), md.gamma)));
+      accept = ratio > raw.acceptance_level;
+      if (err_move) {
+        err_prop++;
+        if (accept) err_acc++;
+      }
+    }
+    // src/Application.hpp:456, best over proposals
+    if (!has_best || pscore > best_score) {
+      has_best = true;
+      best_score = pscore;
+      best_alpha = palpha;
+      best_beta = pbeta;
+      bsk = sk;
+      bsm = sm;
+      copy_rows_part<W32>(scored, gbest, n, wpc, wic, lane);
+    }
+    if (trace != nullptr && wic == 0 && lane == 0) {
+      bbs_step_trace *t = trace + i;
+      t->move = raw;
+      t->proposed_score = pscore;
+      t->current_score = accept ? pscore : score;
+      t->proposed_beta = pbeta;
+      t->accepted = accept ? 1u : 0u;
+      t->proposed_alpha = palpha;
+#pragma unroll
+      for (int k = 0; k < 3; k++) t->reserved[k] = 0;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        t->proposed_counts[k] = SUM ? 0ull : (uint64_t)e[k];
+    }
+    if (accept) {
+      if (!err_move) {
+        uint32_t *t = cur;
+        cur = prop;
+        prop = t;
+      }
+      alpha = palpha;
+      beta = pbeta;
+      score = pscore;
+      prior = pprior;
+      L = PL;
+      geo = pgeo;
+      csk = sk;
+      csm = sm;
+    }
+    __syncwarp();
+  }
+  copy_rows_part<W32>(cur, g, n, wpc, wic, lane);
+  if (wic == 0 && lane == 0) {
+    ChainState o = st;
+    o.alpha = alpha;
+    o.beta = beta;
+    o.score = score;
+    o.prior = prior;
+    o.l00 = L.l00;
+    o.l10 = L.l10;
+    o.l01 = L.l01;
+    o.l11 = L.l11;
+    o.grad_a = geo.grad_a;
+    o.grad_b = geo.grad_b;
+    o.prec_a = geo.prec_a;
+    o.prec_b = geo.prec_b;
+    o.sk = csk;
+    o.sm = csm;
+    o.has_best = has_best ? 1u : 0u;
+    o.best_alpha = best_alpha;
+    o.best_beta = best_beta;
+    o.best_score = best_score;
+    o.best_sk = bsk;
+    o.best_sm = bsm;
+    o.steps_done = st.steps_done + (uint64_t)i;
+    o.err_proposed = err_prop;
+    o.err_accepted = err_acc;
+    *gstate = o;
+    if (cancelled && status != nullptr) atomicOr(status, 1);
+  }
+  if (multi) __syncthreads(); else __syncwarp();
 }
 
 // Resident 128-thread blocks per SM the register budget aims for: fewer
@@ -54,7 +296,9 @@ struct McmcOccupancy {
   static constexpr int min_blocks = Q == 1 ? 4 : (Q == 2 ? 3 : 2);
 };
 
-template <int W32, int Q>
+// One dataset: chains 0..n_chains-1, one warp per chain (blocks of `cpb`
+// chains) or wpc warps per chain (the block is one chain).
+template <int W32, int Q, bool SUM>
 __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
     mcmc_kernel(const RunArgs a) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -69,140 +313,117 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   uint32_t *buf0 = smem + (size_t)slot * slot_words(n, RS, wpc);
   uint32_t *buf1 = buf0 + n * RS;
   int *part = reinterpret_cast<int *>(buf0 + 2 * n * RS);
-  volatile int *sflag = part + 4 * wpc;
-  const bool multi = wpc > 1;  // block-uniform
+  volatile int *sflag = part + 24 * wpc;
   const bool resident = a.ds.n_cells <= 32 * wpc * Q;
   Cells<W32, Q> cb;
   if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
-
   for (int chain = blockIdx.x * cpb + slot; chain < a.n_chains;
        chain += gridDim.x * cpb) {
-    const ChainState st = a.states[chain];
-    uint32_t *g = a.rows + (size_t)chain * n * RS;
-    uint32_t *gbest = a.best_rows + (size_t)chain * n * RS;
-    copy_rows_part<W32>(g, buf0, n, wpc, wic, lane);
-    if (multi) __syncthreads(); else __syncwarp();
-    uint32_t *cur = buf0, *prop = buf1;
-    float beta = st.beta, score = st.score;
-    float l01 = st.l01, l11 = st.l11, prior = st.prior;
-    int csk = st.sk, csm = st.sm;
-    bool has_best = st.has_best != 0;
-    float best_score = st.best_score, best_beta = st.best_beta;
-    int bsk = st.best_sk, bsm = st.best_sm;
-    int i = 0;
-    bool cancelled = false;
-    for (; i < a.n_steps; i++) {
-      if (a.cancel != nullptr && (i & 255) == 0) {
-        // one reader, then a chain-uniform decision
-        if (wic == 0 && lane == 0) *sflag = *a.cancel;
-        if (multi) __syncthreads(); else __syncwarp();
-        const int c = *sflag;
-        if (multi) __syncthreads(); else __syncwarp();
-        if (c) {
-          cancelled = true;
-          break;
-        }
-      }
-      const uint64_t step = st.steps_done + (uint64_t)i;
-      const bbs_raw_move raw =
-          a.moves != nullptr
-              ? a.moves[(size_t)chain * a.n_steps + i]
-              : sample_move(a.mp, (uint32_t)n, a.seed, (uint32_t)chain, step,
-                            a.trace != nullptr);
-      uint32_t Dv[W32], Dw[W32];
-      const Realized R = realize_move<W32>(cur, n, beta, raw, lane, Dv, Dw);
-      const bool beta_move = raw.move_type == BBS_MOVE_CHANGE_BETA;
-      const uint32_t *scored = cur;
-      float pbeta = beta, pl01 = l01, pl11 = l11, pprior = prior;
-      if (beta_move) {
-        pbeta = R.p.new_beta;
-        beta_terms(a.ds, pbeta, pl01, pl11, pprior);
-      } else {
-        build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
-                            lane);
-        scored = prop;
-      }
-      if (multi) __syncthreads(); else __syncwarp();
-      int sk, sm;
-      score_part<W32, Q>(scored, n, a.ds, cb, resident, pl01, pl11, wpc, wic,
-                         lane, sk, sm);
-      if (multi) {
-        int *pp = part + (i & 1) * 2 * wpc;
-        if (lane == 0) {
-          pp[2 * wic] = sk;
-          pp[2 * wic + 1] = sm;
-        }
-        __syncthreads();
-        sk = sm = 0;
-        for (int w = 0; w < wpc; w++) {
-          sk += pp[2 * w];
-          sm += pp[2 * w + 1];
-        }
-      }
-      const float pscore = tree_score(a.ds, sk, sm, pl01, pl11, pprior);
-      // src/Application.hpp:443-456
-      float corr = 1.0f;
-      if (raw.move_type == BBS_MOVE_SWAP_SUBTREES && R.related)
-        corr = __fdiv_rn((float)R.ndv, (float)R.ndw);
-      const float ratio = __fmul_rn(
-          corr, expf(__fmul_rn(__fsub_rn(pscore, score), a.gamma)));
-      const bool accept = ratio > raw.acceptance_level;
-      if (!has_best || pscore > best_score) {
-        has_best = true;
-        best_score = pscore;
-        best_beta = pbeta;
-        bsk = sk;
-        bsm = sm;
-        copy_rows_part<W32>(scored, gbest, n, wpc, wic, lane);
-      }
-      if (a.trace != nullptr && wic == 0 && lane == 0) {
-        bbs_step_trace *t = a.trace + (size_t)chain * a.n_steps + i;
-        t->move = raw;
-        t->proposed_score = pscore;
-        t->current_score = accept ? pscore : score;
-        t->proposed_beta = pbeta;
-        t->accepted = accept ? 1u : 0u;
-        int N[4];
-        class_totals(a.ds, sk, sm, N);
-#pragma unroll
-        for (int k = 0; k < 4; k++) t->proposed_counts[k] = (uint64_t)N[k];
-      }
-      if (accept) {
-        if (!beta_move) {
-          uint32_t *t = cur;
-          cur = prop;
-          prop = t;
-        }
-        beta = pbeta;
-        score = pscore;
-        l01 = pl01;
-        l11 = pl11;
-        prior = pprior;
-        csk = sk;
-        csm = sm;
-      }
-      __syncwarp();
-    }
-    copy_rows_part<W32>(cur, g, n, wpc, wic, lane);
-    if (wic == 0 && lane == 0) {
-      ChainState o = st;
-      o.beta = beta;
-      o.score = score;
-      o.l01 = l01;
-      o.l11 = l11;
-      o.prior = prior;
-      o.sk = csk;
-      o.sm = csm;
-      o.has_best = has_best ? 1u : 0u;
-      o.best_beta = best_beta;
-      o.best_score = best_score;
-      o.best_sk = bsk;
-      o.best_sm = bsm;
-      o.steps_done = st.steps_done + (uint64_t)i;
-      a.states[chain] = o;
-      if (cancelled && a.status != nullptr) atomicOr(a.status, 1);
-    }
-    if (multi) __syncthreads(); else __syncwarp();
+    run_chain<W32, Q, SUM>(
+        a.ds, a.md, (uint32_t)chain, a.rows + (size_t)chain * n * RS,
+        a.best_rows + (size_t)chain * n * RS, a.states + chain,
+        a.moves != nullptr ? a.moves + (size_t)chain * a.n_steps : nullptr,
+        a.trace != nullptr ? a.trace + (size_t)chain * a.n_steps : nullptr,
+        a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, cb, resident,
+        wpc, wic, lane);
+  }
+}
+
+// Many datasets: warps take chains from a shared work list (costliest
+// first); each chain brings its own dataset and rules.  One warp per chain.
+template <int W32, int Q, bool SUM>
+__global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
+    batch_kernel(const BatchArgs b) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  constexpr int RS = rs_of_w32(W32);
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  uint32_t *buf0 = smem + (size_t)wib * slot_words(b.max_nodes, RS, 1);
+  uint32_t *buf1 = buf0 + b.max_nodes * RS;
+  int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
+  volatile int *sflag = part + 24;
+  Cells<W32, Q> cb;
+  for (;;) {
+    unsigned int unit = 0;
+    if (lane == 0) unit = atomicAdd(b.next_unit, 1u);
+    unit = __shfl_sync(BBS_FULL_MASK, unit, 0);
+    if (unit >= (unsigned int)b.n_units) break;
+    const uint32_t chain = b.units[unit];
+    const uint32_t d = b.chain_ds[chain];
+    const DatasetDev ds = b.ds[d];
+    const ModelDev md = b.md[d];
+    // the dataset's node count is within this launch's row width
+    uint32_t *buf1d = buf0 + ds.n_nodes * RS;
+    const bool resident = ds.n_cells <= 32 * Q;
+    if (resident) load_cells<W32, Q>(cb, ds, 0, 32, lane);
+    const uint64_t off = b.chain_off[chain];
+    // Philox key: the chain's number within its dataset, so a dataset's
+    // chains draw the same moves here as in a one-dataset run.
+    const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
+    run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
+                           b.states + chain, nullptr, nullptr, b.n_steps,
+                           b.cancel, b.status, buf0, buf1d, part, sflag, cb,
+                           resident, 1, 0, lane);
+    (void)buf1;
+  }
+}
+
+// Initial chain states: each chain's tree evaluated at (alpha_mean,
+// beta_mean); one warp per chain.
+template <int W32, int Q, bool SUM>
+__global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  constexpr int RS = rs_of_w32(W32);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const int idx = blockIdx.x * wpb + wib;
+  if (idx >= a.n_chains) return;  // whole warp
+  const int chain = a.chain_list != nullptr ? (int)a.chain_list[idx] : idx;
+  const uint32_t d = a.chain_ds != nullptr ? a.chain_ds[chain] : 0u;
+  const DatasetDev ds = a.ds[d];
+  const ModelDev md = a.md[d];
+  const int n = ds.n_nodes;
+  const uint64_t off = a.chain_off != nullptr ? a.chain_off[chain]
+                                              : (uint64_t)chain * n * RS;
+  uint32_t *rows = smem + (size_t)wib * a.max_nodes * RS;
+  copy_rows<W32>(a.rows + off, rows, n, lane);
+  __syncwarp();
+  const float *tm = a.terms + 8 * (size_t)d;
+  const LogTable L{tm[2], tm[3], tm[4], tm[5]};
+  const float alpha = tm[0], beta = tm[1], prior = tm[6];
+  Cells<W32, Q> cb;
+  float e[4];
+  int sk, sm;
+  const float S = evaluate<W32, Q, SUM>(rows, n, ds, cb, false, L, prior, 1, 0,
+                                        lane, nullptr, 0, e, sk, sm);
+  if (lane == 0) {
+    const ErrorGeom geo = error_geometry(ds, alpha, beta, md.gamma, e);
+    ChainState o;
+    o.alpha = alpha;
+    o.beta = beta;
+    o.score = S;
+    o.prior = prior;
+    o.l00 = L.l00;
+    o.l10 = L.l10;
+    o.l01 = L.l01;
+    o.l11 = L.l11;
+    o.grad_a = geo.grad_a;
+    o.grad_b = geo.grad_b;
+    o.prec_a = geo.prec_a;
+    o.prec_b = geo.prec_b;
+    o.sk = sk;
+    o.sm = sm;
+    o.has_best = 0;
+    o.best_alpha = alpha;
+    o.best_beta = beta;
+    o.best_score = -INFINITY;
+    o.best_sk = 0;
+    o.best_sm = 0;
+    o.steps_done = 0;
+    o.err_proposed = 0;
+    o.err_accepted = 0;
+    for (int k = 0; k < 8; k++) o.pad[k] = 0;
+    a.states[chain] = o;
   }
 }
 
@@ -219,13 +440,14 @@ __global__ void __launch_bounds__(128) score_kernel(const ScoreArgs a) {
   copy_rows<W32>(a.rows + (size_t)tree * n * RS, rows, n, lane);
   __syncwarp();
   const float *bt = a.beta_terms + 4 * (size_t)tree;
-  const float l01 = bt[1], l11 = bt[2], prior = bt[3];
+  const LogTable L{a.ds.l00, a.ds.l10, bt[1], bt[2]};
+  const float prior = bt[3];
   Cells<W32, Q> cb;
   int k = 0, m = 0;
   for (int c0 = 0; c0 < a.ds.n_cells; c0 += 32 * Q) {
     load_cells<W32, Q>(cb, a.ds, c0, 32, lane);
     int bj[Q];
-    best_nodes<W32, Q>(rows, n, cb, a.ds.l00, l01, a.ds.l10, l11, bj);
+    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
     counts_at<W32, Q>(rows, cb, bj, k, m);
     if constexpr (ATTACH) {
 #pragma unroll
@@ -239,30 +461,12 @@ __global__ void __launch_bounds__(128) score_kernel(const ScoreArgs a) {
   const int sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);
   const int sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
   if (lane == 0) {
-    const float s = tree_score(a.ds, sk, sm, l01, l11, prior);
+    const float s = tree_score(a.ds, sk, sm, L, prior);
     if (a.scores) a.scores[tree] = s;
     if (a.counts) {
       int N[4];
       class_totals(a.ds, sk, sm, N);
       for (int q = 0; q < 4; q++) a.counts[4 * (size_t)tree + q] = (uint64_t)N[q];
-    }
-    if (a.states) {
-      ChainState o;
-      o.beta = bt[0];
-      o.score = s;
-      o.l01 = l01;
-      o.l11 = l11;
-      o.prior = prior;
-      o.sk = sk;
-      o.sm = sm;
-      o.has_best = 0;
-      o.best_beta = bt[0];
-      o.best_score = -INFINITY;
-      o.best_sk = 0;
-      o.best_sm = 0;
-      o.steps_done = 0;
-      o.pad[0] = o.pad[1] = 0;
-      a.states[tree] = o;
     }
   }
 }

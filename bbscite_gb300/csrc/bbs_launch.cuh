@@ -18,7 +18,7 @@ inline cudaError_t prepare_smem(K kernel, size_t smem) {
 // Persistent launch.  wpc == 1: blocks of `cpb` one-warp chains; wpc > 1:
 // blocks of one chain of wpc warps.  As many blocks as chains need, capped
 // at what stays resident; each block then walks its chain slots.
-template <int W32, int Q>
+template <int W32, int Q, bool SUM>
 int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   if (a.wpc > 1) cpb = 1;
@@ -26,22 +26,47 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   if (threads > 128) return (int)cudaErrorInvalidConfiguration;
   const size_t smem =
       (size_t)cpb * slot_words(a.ds.n_nodes, RS, a.wpc) * sizeof(uint32_t);
-  cudaError_t e = prepare_smem(mcmc_kernel<W32, Q>, smem);
+  auto kern = mcmc_kernel<W32, Q, SUM>;
+  cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mcmc_kernel<W32, Q>,
-                                                    threads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
   if (e != cudaSuccess) return (int)e;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
   const int want = (a.n_chains + cpb - 1) / cpb;
   const int blocks = std::max(1, std::min(want, per_sm * n_sms));
-  mcmc_kernel<W32, Q><<<blocks, threads, smem, s>>>(a);
+  kern<<<blocks, threads, smem, s>>>(a);
   return (int)cudaGetLastError();
 }
 
-int launch_mcmc_lo(const RunArgs &a, int w32, int q, int cpb, int n_sms,
-                   cudaStream_t s);
-int launch_mcmc_hi(const RunArgs &a, int w32, int q, int cpb, int n_sms,
-                   cudaStream_t s);
+// Work-list launch: enough resident warps to fill the GPU, never more than
+// there are units.
+template <int W32, int Q, bool SUM>
+int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
+  constexpr int RS = rs_of_w32(W32);
+  const int threads = 32 * wpb;
+  const size_t smem =
+      (size_t)wpb * slot_words(b.max_nodes, RS, 1) * sizeof(uint32_t);
+  auto kern = batch_kernel<W32, Q, SUM>;
+  cudaError_t e = prepare_smem(kern, smem);
+  if (e != cudaSuccess) return (int)e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+  if (e != cudaSuccess) return (int)e;
+  if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
+  const int want = (b.n_units + wpb - 1) / wpb;
+  const int blocks = std::max(1, std::min(want, per_sm * n_sms));
+  kern<<<blocks, threads, smem, s>>>(b);
+  return (int)cudaGetLastError();
+}
+
+int launch_mcmc_lo(const RunArgs &a, int w32, int q, bool sum, int cpb,
+                   int n_sms, cudaStream_t s);
+int launch_mcmc_hi(const RunArgs &a, int w32, int q, bool sum, int cpb,
+                   int n_sms, cudaStream_t s);
+int launch_batch_lo(const BatchArgs &b, int w32, int q, bool sum, int wpb,
+                    int n_sms, cudaStream_t s);
+int launch_batch_hi(const BatchArgs &b, int w32, int q, bool sum, int wpb,
+                    int n_sms, cudaStream_t s);
 
 }  // namespace bbs

@@ -3,14 +3,14 @@
 
 namespace bbs {
 
-#define BBS_Q_CASES(W)                                        \
-  case W * 10 + 1: return launch_mcmc_t<W, 1>(a, cpb, n_sms, s); \
-  case W * 10 + 2: return launch_mcmc_t<W, 2>(a, cpb, n_sms, s); \
-  case W * 10 + 3: return launch_mcmc_t<W, 3>(a, cpb, n_sms, s); \
-  case W * 10 + 4: return launch_mcmc_t<W, 4>(a, cpb, n_sms, s);
+#define BBS_CASE(W, QQ)                                                   \
+  case W * 10 + QQ:                                                       \
+    return sum ? launch_mcmc_t<W, QQ, true>(a, cpb, n_sms, s)             \
+               : launch_mcmc_t<W, QQ, false>(a, cpb, n_sms, s);
+#define BBS_Q_CASES(W) BBS_CASE(W, 1) BBS_CASE(W, 2) BBS_CASE(W, 3) BBS_CASE(W, 4)
 
-int launch_mcmc_lo(const RunArgs &a, int w32, int q, int cpb, int n_sms,
-                   cudaStream_t s) {
+int launch_mcmc_lo(const RunArgs &a, int w32, int q, bool sum, int cpb,
+                   int n_sms, cudaStream_t s) {
   switch (w32 * 10 + q) {
     BBS_Q_CASES(1)
     BBS_Q_CASES(2)

@@ -30,8 +30,13 @@ MOVE_PARAMS = np.dtype([("move_type", "<i4"), ("v", "<u4"), ("w", "<u4"),
                         ("nondescendant_of_v", "<u4"), ("new_beta", "<f4")])
 STEP_TRACE = np.dtype([("move", RAW_MOVE), ("proposed_score", "<f4"),
                        ("current_score", "<f4"), ("proposed_beta", "<f4"),
-                       ("accepted", "<u4"), ("proposed_counts", "<u8", (4,))])
-assert RAW_MOVE.itemsize == 32 and STEP_TRACE.itemsize == 80
+                       ("accepted", "<u4"), ("proposed_alpha", "<f4"),
+                       ("reserved", "<u4", (3,)),
+                       ("proposed_counts", "<u8", (4,))])
+assert RAW_MOVE.itemsize == 32 and STEP_TRACE.itemsize == 96
+
+SCORE_MAX, SCORE_SUM = 0, 1
+ERROR_BETA_WALK, ERROR_RANDOM_WALK, ERROR_LANGEVIN = 0, 1, 2
 
 
 class BbsError(RuntimeError):
@@ -47,7 +52,9 @@ class Params(C.Structure):
                 ("prob_swap_nodes", C.c_float),
                 ("prob_swap_subtrees", C.c_float),
                 ("beta_jump_scaling_chi", C.c_float), ("gamma", C.c_float),
-                ("reserved0", C.c_uint32), ("seed", C.c_uint64)]
+                ("reserved0", C.c_uint32), ("seed", C.c_uint64),
+                ("score_mode", C.c_uint32), ("error_move", C.c_uint32),
+                ("error_step", C.c_float), ("reserved1", C.c_uint32)]
 
 
 _lib = None
@@ -89,7 +96,17 @@ def lib():
         "bbs_get_launch": (C.c_int, [v, v, v, v]),
         "bbs_autotune": (C.c_int, [v, u32, v]),
         "bbs_get_best": (C.c_int, [v, v, v, v, v, v, v, v]),
-        "bbs_get_chains": (C.c_int, [v, v, v, v, v]),
+        "bbs_get_chains": (C.c_int, [v, v, v, v, v, v, v]),
+        "bbs_get_best_alpha": (C.c_int, [v, v]),
+        "bbs_batch_create": (C.c_int, [v, u32, v, v, v, v, v]),
+        "bbs_batch_destroy": (None, [v]),
+        "bbs_batch_init_chains": (C.c_int, [v, u32]),
+        "bbs_batch_run": (C.c_int, [v, u32]),
+        "bbs_batch_last_run_ms": (C.c_int, [v, v]),
+        "bbs_batch_set_launch": (C.c_int, [v, C.c_int, C.c_int, C.c_int]),
+        "bbs_batch_get_launch": (C.c_int, [v, v, v, v]),
+        "bbs_batch_autotune": (C.c_int, [v, u32, v]),
+        "bbs_batch_get_best": (C.c_int, [v, u32, v, v, v, v, v]),
         "bbs_score_trees": (C.c_int, [v, v, v, u32, v, v, v]),
         "bbs_apply_moves": (C.c_int, [v, v, v, u32, v, v, v, v, v]),
         "bbs_sumscore_grad": (C.c_int, [v, v, v, v, u32, v, v, v, v]),
@@ -295,12 +312,20 @@ class Context:
 
     def chains(self) -> dict:
         dm = np.zeros((self.n_chains, self.n_nodes, self.W), dtype=np.uint64)
+        alpha = np.zeros(self.n_chains, dtype=np.float32)
         beta = np.zeros(self.n_chains, dtype=np.float32)
         score = np.zeros(self.n_chains, dtype=np.float32)
         counts = np.zeros((self.n_chains, 4), dtype=np.uint64)
-        check(lib().bbs_get_chains(self._h, _p(dm), _p(beta), _p(score),
-                                   _p(counts)))
-        return dict(dm=dm, beta=beta, score=score, counts=counts)
+        err = np.zeros((self.n_chains, 2), dtype=np.uint32)
+        check(lib().bbs_get_chains(self._h, _p(dm), _p(alpha), _p(beta),
+                                   _p(score), _p(counts), _p(err)))
+        return dict(dm=dm, alpha=alpha, beta=beta, score=score,
+                    counts=counts, err_stats=err)
+
+    def best_alpha(self) -> float:
+        a = C.c_float()
+        check(lib().bbs_get_best_alpha(self._h, C.byref(a)))
+        return a.value
 
     # -- batch primitives --
     def score_trees(self, dm, betas, attach: bool = False):
@@ -349,3 +374,83 @@ class Context:
                                       n_trees, _p(logl), _p(da), _p(db),
                                       _p(post)))
         return logl, da, db, post
+
+
+class Batch:
+    """Many datasets whose chains run in one launch per row width."""
+
+    def __init__(self, datasets, params):
+        """datasets: list of (mut, known, n_cells, n_genes); params: one
+        Params or a list of one per dataset."""
+        n = len(datasets)
+        if isinstance(params, Params):
+            params = [params] * n
+        self._keep = []
+        self.n_datasets = n
+        self.n_cells = np.array([d[2] for d in datasets], dtype=np.uint32)
+        self.n_genes = np.array([d[3] for d in datasets], dtype=np.uint32)
+        muts = (C.c_void_p * n)()
+        knowns = (C.c_void_p * n)()
+        for i, (mut, known, _, _) in enumerate(datasets):
+            mu = np.ascontiguousarray(mut, dtype=np.uint64)
+            kn = np.ascontiguousarray(known, dtype=np.uint64)
+            self._keep += [mu, kn]
+            muts[i] = mu.ctypes.data
+            knowns[i] = kn.ctypes.data
+        parr = (Params * n)(*params)
+        h = C.c_void_p()
+        check(lib().bbs_batch_create(C.byref(h), n, _p(self.n_cells),
+                                     _p(self.n_genes), muts, knowns, parr))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().bbs_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def init_chains(self, chains_per_dataset: int) -> None:
+        check(lib().bbs_batch_init_chains(self._h, chains_per_dataset))
+
+    def run(self, n_steps: int) -> None:
+        check(lib().bbs_batch_run(self._h, n_steps))
+
+    def last_run_ms(self) -> float:
+        ms = C.c_float()
+        check(lib().bbs_batch_last_run_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def set_launch(self, cells_per_lane=0, warps_per_block=0,
+                   merge_rows=-1) -> None:
+        check(lib().bbs_batch_set_launch(self._h, cells_per_lane,
+                                         warps_per_block, merge_rows))
+
+    def launch(self) -> tuple:
+        q, w, m = C.c_int(), C.c_int(), C.c_int()
+        check(lib().bbs_batch_get_launch(self._h, C.byref(q), C.byref(w),
+                                         C.byref(m)))
+        return q.value, w.value, m.value
+
+    def autotune(self, probe_steps: int = 64) -> float:
+        ms = C.c_float()
+        check(lib().bbs_batch_autotune(self._h, probe_steps, C.byref(ms)))
+        return ms.value
+
+    def best(self, dataset: int) -> dict:
+        n = int(self.n_genes[dataset]) + 1
+        dm = np.zeros((n, words(n)), dtype=np.uint64)
+        parent = np.zeros(n, dtype=np.uint32)
+        a, b, s = C.c_float(), C.c_float(), C.c_float()
+        check(lib().bbs_batch_get_best(self._h, dataset, _p(dm), _p(parent),
+                                       C.byref(a), C.byref(b), C.byref(s)))
+        return dict(dm=dm, parent=parent, alpha=a.value, beta=b.value,
+                    score=s.value)
+

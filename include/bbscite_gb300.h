@@ -68,7 +68,28 @@ typedef struct bbs_params {
   float gamma;                 /* -g   */
   uint32_t reserved0;
   uint64_t seed; /* Philox key for moves and random initial trees */
+  /* Extensions without a counterpart in the reference (defaults reproduce
+   * it): the score and the error-rate move taken with probability
+   * prob_beta_change. */
+  uint32_t score_mode; /* BBS_SCORE_MAX (reference) or BBS_SCORE_SUM */
+  uint32_t error_move; /* BBS_ERROR_BETA_WALK (reference), _RANDOM_WALK,
+                          _LANGEVIN */
+  float error_step;    /* step of the learned error moves (preconditioned) */
+  uint32_t reserved1;
 } bbs_params;
+
+/* Score: the reference's max over attachments (src/TreeScorer.hpp:131-210)
+ * or the sum over attachments, log sum_j exp s_cj per cell. */
+#define BBS_SCORE_MAX 0
+#define BBS_SCORE_SUM 1
+/* Error-rate move: the reference's beta random walk reflected into [0,1]
+ * (src/MutationTree.hpp:345-351, sd = beta_sd / chi); a preconditioned
+ * random walk on (logit alpha, logit beta); or a Langevin (MALA) step
+ * driven by the adjoint gradient of the score.  The last two learn alpha
+ * as well and accept with the exact Metropolis-Hastings ratio. */
+#define BBS_ERROR_BETA_WALK 0
+#define BBS_ERROR_RANDOM_WALK 1
+#define BBS_ERROR_LANGEVIN 2
 
 /* One recorded move, src/RawMoveDistribution.hpp:44-50 (32 bytes). */
 typedef struct bbs_raw_move {
@@ -95,7 +116,9 @@ typedef struct bbs_step_trace {
   float current_score;    /* chain score after the step */
   float proposed_beta;
   uint32_t accepted;
-  uint64_t proposed_counts[4]; /* class totals n00,n01,n10,n11 */
+  float proposed_alpha;
+  uint32_t reserved[3];
+  uint64_t proposed_counts[4]; /* class totals n00,n01,n10,n11 (max score) */
 } bbs_step_trace;
 
 typedef struct bbs_ctx bbs_ctx;
@@ -196,9 +219,14 @@ BBS_API int bbs_last_run_ms(const bbs_ctx *ctx, float *ms);
 BBS_API int bbs_get_best(bbs_ctx *ctx, uint64_t *am, uint64_t *dm, uint32_t *parent,
                  float *beta, float *score, uint64_t *counts,
                  uint32_t *chain);
-/* Current chain states (dm rows n_chains x n_nodes x W, betas, scores). */
-BBS_API int bbs_get_chains(bbs_ctx *ctx, uint64_t *dm, float *beta, float *score,
-                   uint64_t *counts);
+/* The alpha of the best proposal (equal to alpha_mean unless alpha is
+ * learned by the error move). */
+BBS_API int bbs_get_best_alpha(bbs_ctx *ctx, float *alpha);
+/* Current chain states (dm rows n_chains x n_nodes x W, alphas, betas,
+ * scores, class totals); error-move statistics (proposed, accepted) per
+ * chain in err_stats (n_chains x 2).  Any output may be NULL. */
+BBS_API int bbs_get_chains(bbs_ctx *ctx, uint64_t *dm, float *alpha, float *beta,
+                   float *score, uint64_t *counts, uint32_t *err_stats);
 
 /* TreeScorer::logscore_tree for a batch, src/TreeScorer.hpp:131-210:
  * dm = n_trees x n_nodes x W ancestor rows, betas (n_trees).  Outputs:
@@ -219,6 +247,42 @@ BBS_API int bbs_apply_moves(bbs_ctx *ctx, const uint64_t *dm, const float *betas
                     const bbs_move_params *params,
                     bbs_move_params *params_out, uint64_t *dm_out,
                     float *beta_out);
+
+/* ---- many datasets in one launch (no counterpart in the reference,
+ * whose FPGA build takes one dataset per run) ----
+ * Datasets of up to BBS_MAX_GENES genes, each with its own cells and
+ * parameters; chains of all datasets run in one persistent launch per
+ * row-width group, taken costliest first from a shared work list. */
+typedef struct bbs_batch bbs_batch;
+/* is_mutated[d] / is_known[d]: n_cells[d] x bbs_words(n_genes[d] + 1). */
+BBS_API int bbs_batch_create(bbs_batch **batch, uint32_t n_datasets,
+                             const uint32_t *n_cells, const uint32_t *n_genes,
+                             const uint64_t *const *is_mutated,
+                             const uint64_t *const *is_known,
+                             const bbs_params *params);
+BBS_API void bbs_batch_destroy(bbs_batch *batch);
+/* chains_per_dataset random initial trees per dataset (from each
+ * dataset's seed). */
+BBS_API int bbs_batch_init_chains(bbs_batch *batch, uint32_t chains_per_dataset);
+/* Advances every chain by n_steps; the launches are replayed from a CUDA
+ * graph captured on the first run with this n_steps. */
+BBS_API int bbs_batch_run(bbs_batch *batch, uint32_t n_steps);
+BBS_API int bbs_batch_last_run_ms(const bbs_batch *batch, float *ms);
+/* Launch shape: cells per lane (1, 2 or 4) and warps per block (1-4);
+ * merge_rows != 0 runs 1- and 3-word trees with their 2- and 4-word row
+ * stride group (one launch per group instead of two). */
+BBS_API int bbs_batch_set_launch(bbs_batch *batch, int cells_per_lane,
+                                 int warps_per_block, int merge_rows);
+BBS_API int bbs_batch_get_launch(const bbs_batch *batch, int *cells_per_lane,
+                                 int *warps_per_block, int *merge_rows);
+/* Times probe_steps steps per launch shape (chain states restored) and
+ * keeps the fastest. */
+BBS_API int bbs_batch_autotune(bbs_batch *batch, uint32_t probe_steps,
+                               float *best_ms);
+/* Best proposal of one dataset (over its chains). */
+BBS_API int bbs_batch_get_best(bbs_batch *batch, uint32_t dataset, uint64_t *dm,
+                               uint32_t *parent, float *alpha, float *beta,
+                               float *score);
 
 /* Sum-over-attachments score and its adjoint (no counterpart in the
  * reference; SCITE's "-s" score, see docs/thesis/chapters/conclusion/

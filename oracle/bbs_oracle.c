@@ -548,6 +548,101 @@ double orc_sumscore_grad_f64(double alpha, double beta, const uint64_t *dm,
   return total;
 }
 
+/* Per-(cell,node) class counts. */
+static void pair_counts(const uint64_t *K, const uint64_t *M,
+                        const uint64_t *A, uint32_t W, double n[4]) {
+  uint32_t c[4] = {0, 0, 0, 0};
+  for (uint32_t k = 0; k < W; k++) {
+    c[0] += (uint32_t)popc64(K[k] & ~M[k] & ~A[k]);
+    c[1] += (uint32_t)popc64(K[k] & ~M[k] & A[k]);
+    c[2] += (uint32_t)popc64(K[k] & M[k] & ~A[k]);
+    c[3] += (uint32_t)popc64(K[k] & M[k] & A[k]);
+  }
+  for (int q = 0; q < 4; q++)
+    n[q] = (double)c[q];
+}
+
+double orc_sumscore_counts_f64(double alpha, double beta, const uint64_t *dm,
+                               uint32_t n_nodes, const uint64_t *mut,
+                               const uint64_t *known, uint32_t n_cells,
+                               double *e) {
+  const double L[4] = {log(1.0 - alpha), log(beta), log(alpha),
+                       log(1.0 - beta)};
+  uint32_t W = orc_words(n_nodes);
+  double *sc = (double *)malloc(sizeof(double) * n_nodes);
+  double *cn = (double *)malloc(sizeof(double) * n_nodes * 4);
+  double total = 0.0, acc[4] = {0, 0, 0, 0};
+  for (uint32_t c = 0; c < n_cells; c++) {
+    const uint64_t *M = mut + (size_t)c * W, *K = known + (size_t)c * W;
+    double mx = -INFINITY;
+    for (uint32_t j = 0; j < n_nodes; j++) {
+      pair_counts(K, M, dm + (size_t)j * W, W, cn + 4 * j);
+      double s = 0.0;
+      for (int q = 0; q < 4; q++)
+        s += cn[4 * j + q] * L[q];
+      sc[j] = s;
+      if (s > mx)
+        mx = s;
+    }
+    double z = 0.0;
+    for (uint32_t j = 0; j < n_nodes; j++)
+      z += exp(sc[j] - mx);
+    total += mx + log(z);
+    for (uint32_t j = 0; j < n_nodes; j++) {
+      const double pi = exp(sc[j] - mx) / z;
+      for (int q = 0; q < 4; q++)
+        acc[q] += pi * cn[4 * j + q];
+    }
+  }
+  free(sc);
+  free(cn);
+  if (e)
+    for (int q = 0; q < 4; q++)
+      e[q] = acc[q];
+  return total;
+}
+
+double orc_maxscore_counts_f64(double alpha, double beta, const uint64_t *dm,
+                               uint32_t n_nodes, const uint64_t *mut,
+                               const uint64_t *known, uint32_t n_cells,
+                               double *e) {
+  const double L[4] = {log(1.0 - alpha), log(beta), log(alpha),
+                       log(1.0 - beta)};
+  uint32_t W = orc_words(n_nodes);
+  double total = 0.0, acc[4] = {0, 0, 0, 0};
+  for (uint32_t c = 0; c < n_cells; c++) {
+    const uint64_t *M = mut + (size_t)c * W, *K = known + (size_t)c * W;
+    double best = -INFINITY, bn[4] = {0, 0, 0, 0};
+    for (uint32_t j = 0; j < n_nodes; j++) {
+      double n[4];
+      pair_counts(K, M, dm + (size_t)j * W, W, n);
+      double s = 0.0;
+      for (int q = 0; q < 4; q++)
+        s += n[q] * L[q];
+      if (j == 0 || s > best) {
+        best = s;
+        memcpy(bn, n, sizeof(bn));
+      }
+    }
+    total += best;
+    for (int q = 0; q < 4; q++)
+      acc[q] += bn[q];
+  }
+  if (e)
+    for (int q = 0; q < 4; q++)
+      e[q] = acc[q];
+  return total;
+}
+
+double orc_logprior_beta_f64(double beta_mean, double beta_sd, double beta) {
+  const double a = ((1.0 - beta_mean) * beta_mean * beta_mean /
+                    (beta_sd * beta_sd)) -
+                   beta_mean;
+  const double b = a * (1.0 / beta_mean - 1.0);
+  return lgamma(a + b) + (a - 1.0) * log(beta) + (b - 1.0) * log(1.0 - beta) -
+         lgamma(a) - lgamma(b);
+}
+
 /* ------------------------------------------------------------------ */
 /* Chain driver                                                        */
 /* ------------------------------------------------------------------ */

@@ -124,6 +124,21 @@ double orc_sumscore_grad_f64(double alpha, double beta, const uint64_t *dm,
                              double *dalpha, double *dbeta,
                              double *posterior);
 
+/* FP64 sum score logL = sum_c logsumexp_j s_cj (no prior) and the expected
+ * class counts e[4] = sum_c sum_j pi_cj (n00, n01, n10, n11). */
+double orc_sumscore_counts_f64(double alpha, double beta, const uint64_t *dm,
+                               uint32_t n_nodes, const uint64_t *mut,
+                               const uint64_t *known, uint32_t n_cells,
+                               double *e);
+/* FP64 class totals at the first-max attachment of the max score. */
+double orc_maxscore_counts_f64(double alpha, double beta, const uint64_t *dm,
+                               uint32_t n_nodes, const uint64_t *mut,
+                               const uint64_t *known, uint32_t n_cells,
+                               double *e);
+/* FP64 log Beta prior of beta with the reference's parameters from
+ * (beta_mean, beta_sd), src/TreeScorer.hpp:108-126. */
+double orc_logprior_beta_f64(double beta_mean, double beta_sd, double beta);
+
 /* ---- chain driver (src/Application.hpp:408-487) ---- */
 typedef struct {
   float alpha_mean, beta_mean, beta_sd, gamma;

@@ -121,6 +121,12 @@ def lib():
         _lib.orc_sumscore_grad_f64.restype = C.c_double
         _lib.orc_sumscore_grad_f64.argtypes = [
             C.c_double, C.c_double, v, u32, v, v, u32, v, v, v]
+        for fn in ("orc_sumscore_counts_f64", "orc_maxscore_counts_f64"):
+            getattr(_lib, fn).restype = C.c_double
+            getattr(_lib, fn).argtypes = [C.c_double, C.c_double, v, u32, v,
+                                          v, u32, v]
+        _lib.orc_logprior_beta_f64.restype = C.c_double
+        _lib.orc_logprior_beta_f64.argtypes = [C.c_double] * 3
         _lib.orc_run_chain.argtypes = [v, u32, v, v, u32, v, u32, v, v, v, v,
                                        v, v, v, v, v, v, v, f32]
         _lib.orc_philox4x32_10.argtypes = [v, v, v]
@@ -267,6 +273,21 @@ def sumscore_grad_f64(alpha, beta, dm, mut, known, posterior=False):
                                     _p(mut), _p(known), mut.shape[0],
                                     C.byref(da), C.byref(db), _p(post))
     return float(r), float(da.value), float(db.value), post
+
+
+def score_counts_f64(alpha, beta, dm, mut, known, sum_score: bool):
+    """FP64 (sum or max) score without prior and its (expected) class
+    counts (n00, n01, n10, n11)."""
+    e = np.zeros(4, dtype=np.float64)
+    fn = (lib().orc_sumscore_counts_f64 if sum_score
+          else lib().orc_maxscore_counts_f64)
+    r = fn(alpha, beta, _p(dm), dm.shape[0], _p(mut), _p(known),
+           mut.shape[0], _p(e))
+    return float(r), e
+
+
+def logprior_beta_f64(beta_mean, beta_sd, beta) -> float:
+    return float(lib().orc_logprior_beta_f64(beta_mean, beta_sd, beta))
 
 
 def move_probs(prob_beta_change=0.0, prob_prune=0.55, prob_swap=0.4,

@@ -1,0 +1,264 @@
+"""Sum score, learned error rates and the batched form, through the C ABI.
+
+Chains run on the GPU with a trace; the host replays every step in FP64
+with the oracle: the proposed tree (bit-exact realisation + update), the
+proposed score (1e-5 relative), the learned-move proposal (drift and
+noise from the recorded uniforms) and the Metropolis-Hastings decision
+(outside a band that covers FP32 score rounding).  The host follows the
+GPU's decisions, and the final trees must match bit for bit.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from bbscite_gb300 import data as D
+
+pytestmark = pytest.mark.gpu
+
+SCORE_RTOL = 1e-5
+
+
+def f32(x):
+    return np.float32(x)
+
+
+def prior_params(beta_mean, beta_sd):
+    a = ((1 - beta_mean) * beta_mean ** 2 / beta_sd ** 2) - beta_mean
+    return a, a * (1 / beta_mean - 1)
+
+
+def geometry(alpha, beta, e, gamma, A, B):
+    va, vb = alpha * (1 - alpha), beta * (1 - beta)
+    dS_da = -e[0] / (1 - alpha) + e[2] / alpha
+    dS_db = (e[1] / beta - e[3] / (1 - beta) + (A - 1) / beta -
+             (B - 1) / (1 - beta))
+    ga = gamma * va * dS_da + (1 - 2 * alpha)
+    gb = gamma * vb * dS_db + (1 - 2 * beta)
+    pa = 1 / (1 + gamma * (e[0] + e[2]) * va)
+    pb = 1 / (1 + gamma * (e[1] + e[3] + max(A + B - 2, 0.0)) * vb)
+    return ga, gb, pa, pb
+
+
+def log_q(ta, tb, fa, fb, g, eps, drift):
+    h = 0.5 * eps * eps if drift else 0.0
+    ra = ta - fa - h * g[2] * g[0]
+    rb = tb - fb - h * g[3] * g[1]
+    return (-(ra * ra) / (2 * eps * eps * g[2]) -
+            (rb * rb) / (2 * eps * eps * g[3]) -
+            0.5 * (math.log(g[2]) + math.log(g[3])))
+
+
+def logit(p):
+    return math.log(p) - math.log1p(-p)
+
+
+def replay(orc, native, m, p, start, trace, final_dm):
+    """FP64 host replay of one traced chain; returns the number of
+    decisions inside the rounding band."""
+    mut, known = D.matrix_to_bits(m)
+    sum_score = p.score_mode == native.SCORE_SUM
+    gamma, eps = float(p.gamma), float(p.error_step)
+    A, B = prior_params(float(p.beta_mean), float(p.beta_sd))
+    am, dm = orc.parent_to_matrix(start)
+    alpha, beta = f32(p.alpha_mean), f32(p.beta_mean)
+
+    def evaluate(dmx, a, b):
+        s, e = orc.score_counts_f64(float(a), float(b), dmx, mut, known,
+                                    sum_score)
+        return s + orc.logprior_beta_f64(float(p.beta_mean),
+                                         float(p.beta_sd), float(b)), e
+
+    S, e = evaluate(dm, alpha, beta)
+    geo = geometry(float(alpha), float(beta), e, gamma, A, B)
+    ambiguous = 0
+    for t in trace:
+        raw = t["move"]
+        corr = 1.0
+        nam, ndm, pa, pb = am, dm, alpha, beta
+        if raw["move_type"] != 0:
+            mp = orc.realize(am, dm, float(beta), _raw(orc, raw))
+            nam, ndm, _ = orc.apply_move(am, dm, float(beta), mp)
+            v, w = int(mp["v"]), int(mp["w"])
+            if raw["move_type"] == 3 and (int(am[w, v // 64]) >> (v % 64)) & 1:
+                corr = float(f32(orc.n_descendants(am, v)) /
+                             f32(orc.n_descendants(am, w)))
+        elif p.error_move == native.ERROR_BETA_WALK:
+            nb = f32(beta + f32(raw["beta_jump"]))
+            if nb < 0:
+                nb = f32(abs(nb))
+            if nb > 1:
+                nb = f32(nb - f32(f32(2.0) * f32(nb - f32(1.0))))
+            pb = nb
+        else:
+            pa, pb = f32(t["proposed_alpha"]), f32(t["proposed_beta"])
+            # the proposal follows drift + preconditioned noise
+            u1 = max(1.0 - float(raw["raw_descendant_of_v"]), 1e-30)
+            r = math.sqrt(-2 * math.log(u1))
+            z0 = r * math.cos(2 * math.pi * float(raw["raw_nondescendant_of_v"]))
+            z1 = r * math.sin(2 * math.pi * float(raw["raw_nondescendant_of_v"]))
+            h = 0.5 * eps * eps if p.error_move == native.ERROR_LANGEVIN else 0
+            ea = logit(float(alpha)) + h * geo[2] * geo[0] + eps * math.sqrt(geo[2]) * z0
+            eb = logit(float(beta)) + h * geo[3] * geo[1] + eps * math.sqrt(geo[3]) * z1
+            if 1e-6 < pa < 1 - 1e-6 and 1e-6 < pb < 1 - 1e-6:
+                assert abs(logit(float(pa)) - ea) < 2e-3 * max(1, abs(ea))
+                assert abs(logit(float(pb)) - eb) < 2e-3 * max(1, abs(eb))
+        S1, e1 = evaluate(ndm, pa, pb)
+        assert abs(t["proposed_score"] - S1) <= SCORE_RTOL * abs(S1) + 1e-4
+        geo1 = geometry(float(pa), float(pb), e1, gamma, A, B)
+        if raw["move_type"] == 0 and p.error_move != native.ERROR_BETA_WALK:
+            fa, fb = logit(float(alpha)), logit(float(beta))
+            ta, tb = logit(float(pa)), logit(float(pb))
+            drift = p.error_move == native.ERROR_LANGEVIN
+            logr = (gamma * (S1 - S) +
+                    math.log(pa * (1 - pa)) + math.log(pb * (1 - pb)) -
+                    math.log(alpha * (1 - alpha)) - math.log(beta * (1 - beta)) +
+                    log_q(fa, fb, ta, tb, geo1, eps, drift) -
+                    log_q(ta, tb, fa, fb, geo, eps, drift))
+        else:
+            logr = gamma * (S1 - S) + math.log(corr)
+        lu = math.log(max(float(raw["acceptance_level"]), 1e-300))
+        host = logr > lu
+        if bool(t["accepted"]) != host:
+            band = 3e-5 * abs(S) + 2e-3
+            assert abs(logr - lu) < band, (logr, lu)
+            ambiguous += 1
+        if t["accepted"]:
+            am, dm, alpha, beta, S, geo = nam, ndm, pa, pb, S1, geo1
+    assert (dm == final_dm).all()
+    return ambiguous
+
+
+def _raw(orc, raw):
+    out = np.zeros(1, dtype=orc.RAW_MOVE)
+    out.view(np.uint8)[:] = np.frombuffer(raw.tobytes(), dtype=np.uint8)
+    return out[0]
+
+
+CASES = [
+    # (score mode, error move, prob of an error move)
+    ("sum", "beta_walk", 0.1),
+    ("sum", "langevin", 0.25),
+    ("sum", "random_walk", 0.25),
+    ("max", "random_walk", 0.25),
+    ("max", "langevin", 0.25),
+]
+
+
+@pytest.mark.parametrize("score,move,p_err", CASES)
+def test_traced_chains_replay_in_fp64(native, orc, score, move, p_err):
+    G, Cn, chains, steps = 30, 40, 3, 250
+    m, _, _ = D.generate_dataset(101, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    p = native.default_params(
+        alpha_mean=1e-2, beta_mean=0.3, seed=17, prob_beta_change=p_err,
+        score_mode=getattr(native, "SCORE_" + score.upper()),
+        error_move=getattr(native, "ERROR_" + move.upper()))
+    rng = np.random.default_rng(4)
+    starts = np.stack([D.random_parent_vector(rng, G) for _ in range(chains)])
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(chains, starts)
+        tr = c.run(steps, trace=True)
+        final = c.chains()
+    n_err = int((tr["move"]["move_type"] == 0).sum())
+    assert n_err > 0
+    amb = sum(replay(orc, native, m, p, starts[ch], tr[ch], final["dm"][ch])
+              for ch in range(chains))
+    assert amb <= 2
+
+
+@pytest.mark.parametrize("score", ["max", "sum"])
+def test_init_scores_match_fp64(native, orc, score):
+    G, Cn = 95, 96
+    m, _, _ = D.generate_dataset(55, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    p = native.default_params(alpha_mean=1e-3, beta_mean=0.2,
+                              score_mode=getattr(native, "SCORE_" + score.upper()))
+    rng = np.random.default_rng(8)
+    starts = np.stack([D.random_parent_vector(rng, G) for _ in range(16)])
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(16, starts)
+        st = c.chains()
+    for k in range(16):
+        _, dm = orc.parent_to_matrix(starts[k])
+        s, _ = orc.score_counts_f64(1e-3, 0.2, dm, mut, known, score == "sum")
+        s += orc.logprior_beta_f64(0.2, 0.1, 0.2)
+        assert abs(st["score"][k] - s) <= SCORE_RTOL * abs(s)
+
+
+@pytest.mark.parametrize("score,move", [("max", "beta_walk"),
+                                        ("sum", "langevin")])
+def test_batch_equals_single_dataset_runs(native, score, move):
+    """A dataset's chains in the batched launch are bit-identical to the
+    same chains run alone (same Philox keys, same kernel code)."""
+    rng = np.random.default_rng(9)
+    specs = [(int(rng.integers(16, 128)), int(rng.integers(16, 200)))
+             for _ in range(7)] + [(200, 40), (33, 300)]
+    datasets, params = [], []
+    for i, (G, Cn) in enumerate(specs):
+        m, _, _ = D.generate_dataset(300 + i, G, Cn, 1e-3, 0.2, 0.1, 0.0)
+        mut, known = D.matrix_to_bits(m)
+        datasets.append((mut, known, Cn, G))
+        params.append(native.default_params(
+            alpha_mean=float(10 ** rng.uniform(-5, -2)),
+            beta_mean=float(rng.uniform(0.05, 0.45)), seed=1000 + i,
+            prob_beta_change=0.1,
+            score_mode=getattr(native, "SCORE_" + score.upper()),
+            error_move=getattr(native, "ERROR_" + move.upper())))
+    cpd, steps = 5, 120
+    with native.Batch(datasets, params) as b:
+        b.init_chains(cpd)
+        b.run(steps)
+        b.run(steps)  # graph replay
+        bests = [b.best(d) for d in range(len(datasets))]
+    for d, (mut, known, Cn, G) in enumerate(datasets):
+        with native.Context(mut, known, Cn, G, params[d]) as c:
+            c.init_chains(cpd)
+            c.run(steps)
+            c.run(steps)
+            want = c.best()
+        assert bests[d]["score"] == want["score"]
+        assert (bests[d]["dm"] == want["dm"]).all()
+
+
+def test_batch_autotune_and_shapes_agree(native):
+    rng = np.random.default_rng(10)
+    datasets = []
+    for i in range(12):
+        G, Cn = int(rng.integers(16, 128)), int(rng.integers(16, 256))
+        m, _, _ = D.generate_dataset(500 + i, G, Cn, 1e-3, 0.2, 0.1, 0.0)
+        mut, known = D.matrix_to_bits(m)
+        datasets.append((mut, known, Cn, G))
+    p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=3)
+    results = []
+    for shape in ((1, 1, 0), (2, 4, 0), (4, 2, 1), None):
+        with native.Batch(datasets, p) as b:
+            b.init_chains(4)
+            if shape is None:
+                assert b.autotune(40) > 0
+            else:
+                b.set_launch(*shape)
+            b.run(150)
+            results.append([b.best(d)["score"] for d in range(12)])
+    for r in results[1:]:
+        assert r == results[0]
+
+
+def test_langevin_learns_alpha(native):
+    """Data made with alpha=1e-3, beta=0.2; chains start at alpha=1e-2,
+    beta=0.3 and learn both with the Langevin error move."""
+    G, Cn = 40, 120
+    m, _, _ = D.generate_dataset(77, G, Cn, 1e-3, 0.2, 0.05, 0.0)
+    mut, known = D.matrix_to_bits(m)
+    p = native.default_params(alpha_mean=1e-2, beta_mean=0.3, seed=5,
+                              prob_beta_change=0.3,
+                              score_mode=native.SCORE_SUM,
+                              error_move=native.ERROR_LANGEVIN)
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(32)
+        c.run(4000)
+        st = c.chains()
+    assert np.median(st["alpha"]) < 4e-3
+    assert abs(np.median(st["beta"]) - 0.2) < 0.06
+    acc = st["err_stats"][:, 1].sum() / max(1, st["err_stats"][:, 0].sum())
+    assert 0.2 < acc < 0.98
