@@ -1449,7 +1449,7 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.cancel = nullptr;
     a.status = b->d_status;
     a.max_nodes = grp.max_nodes;
-    const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;
+    const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;  // 1, 2 above 128 nodes
     const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");
     BBS_CUDA(cudaEventRecord(b->side_ev[g], b->side[g]), "event");
@@ -1690,8 +1690,8 @@ int bbs_batch_last_run_ms(const bbs_batch *b, float *ms) {
 
 int bbs_batch_set_launch(bbs_batch *b, int q, int wpb, int merge) {
   if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
-  if (q != 0 && q != 1 && q != 2 && q != 4)
-    return fail(BBS_ERR_INPUT, "cells per lane must be 1, 2 or 4");
+  if (q < 0 || q > 4)
+    return fail(BBS_ERR_INPUT, "cells per lane must be 1, 2, 3 or 4");
   if (wpb < 0 || wpb > 4) return fail(BBS_ERR_INPUT, "warps per block must be in [1, 4]");
   if (q) b->q = q;
   if (wpb) b->wpb = wpb;
@@ -1735,7 +1735,7 @@ int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
     float best = 1e30f;
     int bq = b->q, bw = b->wpb, bm = b->merge;
     for (int merge : {0, 1})
-      for (int q : {1, 2, 4})
+      for (int q : {1, 2, 3, 4})
         for (int wpb : {1, 2, 4}) {
           int r = bbs_batch_set_launch(b, q, wpb, merge);
           if (r != BBS_OK) return r;

@@ -14,15 +14,19 @@ int launch_batch_lo(const BatchArgs &b, int w32, int q, bool sum, int wpb,
   switch (w32 * 10 + q) {
     BBS_BCASE(1, 1)
     BBS_BCASE(1, 2)
+    BBS_BCASE(1, 3)
     BBS_BCASE(1, 4)
     BBS_BCASE(2, 1)
     BBS_BCASE(2, 2)
+    BBS_BCASE(2, 3)
     BBS_BCASE(2, 4)
     BBS_BCASE(3, 1)
     BBS_BCASE(3, 2)
+    BBS_BCASE(3, 3)
     BBS_BCASE(3, 4)
     BBS_BCASE(4, 1)
     BBS_BCASE(4, 2)
+    BBS_BCASE(4, 3)
     BBS_BCASE(4, 4)
     default: return (int)cudaErrorInvalidValue;
   }

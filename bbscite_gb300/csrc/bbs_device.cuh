@@ -559,24 +559,43 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
   sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
 }
 
-// Sum-over-attachments pass with its adjoint, for the lane's Q cells:
-// per cell an online logsumexp over nodes carries the softmax-weighted
-// sums of d = popc(D & A) and m = popc(M & A).  Adds to acc[5], in fixed
-// point (2^-20 units, so the result does not depend on how cells are
-// split over lanes and warps): sum_c lse_c and the expected class counts
-// E[n00], E[n01], E[n10], E[n11].
+// Sum-over-attachments pass with its adjoint, for the lane's Q cells.
+// Per cell the scores s_j are summed as exp(s_j - r) against a reference r
+// that depends only on the cell and the log table: r = ub - 72 with ub =
+// pd max(l00, l01) + pm max(l10, l11) >= every s_j, so no term overflows.
+// A cell whose maximum lies more than 80 below r is summed once more
+// against its maximum.  In base-2 units t_j = (s_j - r) log2(e) is affine
+// in (d, m) = (popc(D & A), popc(M & A)), two FMAs per pair.  Adds to
+// acc[6], in fixed point (2^-20 units, so the result does not depend on
+// how cells are split over lanes and warps): sum_c lse_c, the expected
+// class counts E[n00], E[n01], E[n10], E[n11], and sum_c max_j s_cj (the
+// max score).
 inline constexpr float kFixScale = 1048576.0f;  // 2^20
+inline constexpr float kLog2E = 1.44269504088896341f;
+inline constexpr float kLn2 = 0.693147180559945309f;
+
+__device__ __forceinline__ float ex2_approx(float t) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
+  return r;
+}
 
 template <int W32, int Q>
 __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const Cells<W32, Q> &cb,
                                           const LogTable &L, int c0, int stride,
                                           int lane, int n_cells,
-                                          long long (&acc)[5]) {
+                                          long long (&acc)[6]) {
   constexpr int RS = rs_of_w32(W32);
-  float mx[Q], z[Q], ed[Q], em[Q];
+  const float c1 = (L.l01 - L.l00) * kLog2E;  // per counted observed-0 bit
+  const float c2 = (L.l11 - L.l10) * kLog2E;  // per counted observed-1 bit
+  const float u0 = fmaxf(L.l00, L.l01), u1 = fmaxf(L.l10, L.l11);
+  float r[Q], base[Q], mx[Q], z[Q], ed[Q], em[Q];
 #pragma unroll
   for (int q = 0; q < Q; q++) {
+    const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
+    r[q] = fmaf(pd, u0, pm * u1) - 72.0f;
+    base[q] = (fmaf(pd, L.l00, pm * L.l10) - r[q]) * kLog2E;
     mx[q] = -INFINITY;
     z[q] = ed[q] = em[q] = 0.0f;
   }
@@ -586,19 +605,45 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     ld_row<W32>(rows + j * RS, a);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      const int d = masked_popc<W32>(cb.D[q], a);
-      const int m = masked_popc<W32>(cb.M[q], a);
-      const float s = pair_score(d, m, cb.pdb[q], cb.pmb[q], L.l00, L.l01,
-                                 L.l10, L.l11);
-      const float fd = __fsub_rn(__int_as_float(0x4B000000 + d), 8388608.0f);
-      const float fm = __fsub_rn(__int_as_float(0x4B000000 + m), 8388608.0f);
-      const float dl = s - mx[q];
-      const bool up = dl > 0.0f;  // new running maximum
-      const float e = __expf(-fabsf(dl));
-      z[q] = up ? fmaf(z[q], e, 1.0f) : z[q] + e;
-      ed[q] = up ? fmaf(ed[q], e, fd) : fmaf(e, fd, ed[q]);
-      em[q] = up ? fmaf(em[q], e, fm) : fmaf(e, fm, em[q]);
-      mx[q] = up ? s : mx[q];
+      const float fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+      const float fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+      const float t = fmaf(fd, c1, fmaf(fm, c2, base[q]));
+      const float e = ex2_approx(t);
+      mx[q] = fmaxf(mx[q], t);
+      z[q] += e;
+      ed[q] = fmaf(e, fd, ed[q]);
+      em[q] = fmaf(e, fm, em[q]);
+    }
+  }
+  bool bad[Q], any = false;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    bad[q] = !(mx[q] >= -80.0f * kLog2E);
+    any |= bad[q];
+  }
+  if (__any_sync(BBS_FULL_MASK, any)) {
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+      if (bad[q]) {
+        r[q] = fmaf(mx[q], kLn2, r[q]);
+        base[q] -= mx[q];
+        mx[q] = 0.0f;
+        z[q] = ed[q] = em[q] = 0.0f;
+      }
+#pragma unroll 1
+    for (int j = 0; j < n; j++) {
+      uint32_t a[W32];
+      ld_row<W32>(rows + j * RS, a);
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        if (!bad[q]) continue;
+        const float fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+        const float fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+        const float e = ex2_approx(fmaf(fd, c1, fmaf(fm, c2, base[q])));
+        z[q] += e;
+        ed[q] = fmaf(e, fd, ed[q]);
+        em[q] = fmaf(e, fm, em[q]);
+      }
     }
   }
 #pragma unroll
@@ -608,11 +653,12 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     const float inv = 1.0f / z[q];
     const float Ed = ed[q] * inv, Em = em[q] * inv;
     const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
-    acc[0] += __float2ll_rn((mx[q] + logf(z[q])) * kFixScale);
+    acc[0] += __float2ll_rn((r[q] + logf(z[q])) * kFixScale);
     acc[1] += __float2ll_rn((pd - Ed) * kFixScale);  // E[n00]
     acc[2] += __float2ll_rn(Ed * kFixScale);         // E[n01]
     acc[3] += __float2ll_rn((pm - Em) * kFixScale);  // E[n10]
     acc[4] += __float2ll_rn(Em * kFixScale);         // E[n11]
+    acc[5] += __float2ll_rn(fmaf(mx[q], kLn2, r[q]) * kFixScale);  // max
   }
 }
 
@@ -623,9 +669,9 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
                                          const DatasetDev &ds,
                                          Cells<W32, Q> &cb, bool resident,
                                          const LogTable &L, int wpc, int wic,
-                                         int lane, long long (&acc)[5]) {
+                                         int lane, long long (&acc)[6]) {
 #pragma unroll
-  for (int i = 0; i < 5; i++) acc[i] = 0;
+  for (int i = 0; i < 6; i++) acc[i] = 0;
   if (resident) {
     sum_cells<W32, Q>(rows, n, cb, L, 32 * wic, 32 * wpc, lane, ds.n_cells,
                       acc);
@@ -640,7 +686,7 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-    for (int i = 0; i < 5; i++) acc[i] += __shfl_xor_sync(BBS_FULL_MASK, acc[i], off);
+    for (int i = 0; i < 6; i++) acc[i] += __shfl_xor_sync(BBS_FULL_MASK, acc[i], off);
 }
 
 // Class totals (n00, n01, n10, n11) from the sums.

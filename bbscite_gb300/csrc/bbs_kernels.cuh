@@ -49,7 +49,8 @@ __host__ __device__ inline int slot_words(int n, int rs, int wpc) {
 
 // Evaluates a tree for the whole chain (all wpc warps): returns the score
 // S = data term + prior and the (exact or expected) class counts e[4];
-// sk, sm are the class sums of the max score.
+// sk, sm are the class sums of the max score and smax the max score itself
+// (S for the max score; for the sum score, sum_c max_j s_cj + prior).
 template <int W32, int Q, bool SUM>
 __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
                                           const DatasetDev &ds,
@@ -57,7 +58,8 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
                                           const LogTable &L, float prior,
                                           int wpc, int wic, int lane,
                                           int *part, int parity,
-                                          float (&e)[4], int &sk, int &sm) {
+                                          float (&e)[4], int &sk, int &sm,
+                                          float &smax) {
   if constexpr (!SUM) {
     int a, b;
     score_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, a, b);
@@ -80,22 +82,24 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
     class_totals(ds, sk, sm, N);
 #pragma unroll
     for (int i = 0; i < 4; i++) e[i] = (float)N[i];
-    return tree_score(ds, sk, sm, L, prior);
+    smax = tree_score(ds, sk, sm, L, prior);
+    return smax;
   } else {
-    long long acc[5];
+    long long acc[6];
     sum_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, acc);
     if (wpc > 1) {
       long long *pp = reinterpret_cast<long long *>(part) + parity * 6 * wpc;
       if (lane == 0)
-        for (int i = 0; i < 5; i++) pp[6 * wic + i] = acc[i];
+        for (int i = 0; i < 6; i++) pp[6 * wic + i] = acc[i];
       __syncthreads();
-      for (int i = 0; i < 5; i++) acc[i] = 0;
+      for (int i = 0; i < 6; i++) acc[i] = 0;
       for (int w = 0; w < wpc; w++)
-        for (int i = 0; i < 5; i++) acc[i] += pp[6 * w + i];
+        for (int i = 0; i < 6; i++) acc[i] += pp[6 * w + i];
     }
     sk = sm = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) e[i] = (float)((double)acc[i + 1] / kFixScale);
+    smax = __fadd_rn((float)((double)acc[5] / kFixScale), prior);
     return __fadd_rn((float)((double)acc[0] / kFixScale), prior);
   }
 }
@@ -187,11 +191,11 @@ __device__ __forceinline__ void run_chain(
       beta_terms(ds, pbeta, PL.l01, PL.l11, pprior);
     }
     if (multi) __syncthreads(); else __syncwarp();
-    float e[4];
+    float e[4], psmax;
     int sk, sm;
     const float pscore = evaluate<W32, Q, SUM>(scored, n, ds, cb, resident, PL,
                                                pprior, wpc, wic, lane, part,
-                                               i & 1, e, sk, sm);
+                                               i & 1, e, sk, sm, psmax);
     ErrorGeom pgeo = geo;
     if (learn) pgeo = error_geometry(ds, palpha, pbeta, md.gamma, e);
     bool accept;
@@ -216,10 +220,11 @@ __device__ __forceinline__ void run_chain(
         if (accept) err_acc++;
       }
     }
-    // src/Application.hpp:456, best over proposals
-    if (!has_best || pscore > best_score) {
+    // src/Application.hpp:456, best over proposals by the reference's max
+    // score (the chain's own score unless it samples the sum score)
+    if (!has_best || psmax > best_score) {
       has_best = true;
-      best_score = pscore;
+      best_score = psmax;
       best_alpha = palpha;
       best_beta = pbeta;
       bsk = sk;
@@ -234,8 +239,9 @@ __device__ __forceinline__ void run_chain(
       t->proposed_beta = pbeta;
       t->accepted = accept ? 1u : 0u;
       t->proposed_alpha = palpha;
+      t->proposed_max_score = psmax;
 #pragma unroll
-      for (int k = 0; k < 3; k++) t->reserved[k] = 0;
+      for (int k = 0; k < 2; k++) t->reserved[k] = 0;
 #pragma unroll
       for (int k = 0; k < 4; k++)
         t->proposed_counts[k] = SUM ? 0ull : (uint64_t)e[k];
@@ -392,10 +398,10 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
   const LogTable L{tm[2], tm[3], tm[4], tm[5]};
   const float alpha = tm[0], beta = tm[1], prior = tm[6];
   Cells<W32, Q> cb;
-  float e[4];
+  float e[4], smax;
   int sk, sm;
   const float S = evaluate<W32, Q, SUM>(rows, n, ds, cb, false, L, prior, 1, 0,
-                                        lane, nullptr, 0, e, sk, sm);
+                                        lane, nullptr, 0, e, sk, sm, smax);
   if (lane == 0) {
     const ErrorGeom geo = error_geometry(ds, alpha, beta, md.gamma, e);
     ChainState o;

@@ -31,7 +31,8 @@ MOVE_PARAMS = np.dtype([("move_type", "<i4"), ("v", "<u4"), ("w", "<u4"),
 STEP_TRACE = np.dtype([("move", RAW_MOVE), ("proposed_score", "<f4"),
                        ("current_score", "<f4"), ("proposed_beta", "<f4"),
                        ("accepted", "<u4"), ("proposed_alpha", "<f4"),
-                       ("reserved", "<u4", (3,)),
+                       ("proposed_max_score", "<f4"),
+                       ("reserved", "<u4", (2,)),
                        ("proposed_counts", "<u8", (4,))])
 assert RAW_MOVE.itemsize == 32 and STEP_TRACE.itemsize == 96
 

@@ -3,21 +3,26 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-Workload (the headline configuration): 95 genes x 96 cells from the seeded
-generator (alpha=1e-3, beta=0.2, 10% unknown, 2% of true mutations
-recorded as homozygous), 1024 chains, fixed error rates, Philox moves,
-max-over-attachments score.  One bench step = one persistent launch that
-advances every chain by --chain-steps steps; chains continue across
-launches.  Inputs are resident in HBM before the timed region; a 256 MiB
-buffer is written between launches to flush L2.
+Headline (`value`): the batched+adjoint form on 95 genes x 96 cells from
+the seeded generator (alpha=1e-3, beta=0.2, 10% unknown, 2% homozygous):
+1024 chains in the work-list launch, sum-over-attachments score with its
+fused adjoint, Langevin error-rate moves (probability 0.1) learning alpha
+and beta from 1e-2 / 0.3.  `plain` is the one-dataset kernel with the
+reference's max score and fixed rates on the same chains.
+`equal_best_logl` scores both forms' best trees with the reference's max
+score at the generator's rates.  One bench step = one launch advancing
+every chain by --chain-steps steps; chains continue across launches.
+Inputs are resident in HBM before the timed region; a 256 MiB buffer is
+written between launches to flush L2.
 
-Prints one JSON line (rank 0).  `value` is device-timed (CUDA events on the
-library's stream around each launch), `e2e` the same metric through the C
-ABI with host buffers (context creation, host->device copies, the run and
-the device->host read of the best tree inside the timed region).
+`value` is device-timed (CUDA events on the library's stream around each
+launch); `e2e` is the same form through the C ABI with host buffers
+(creation, host->device copies, the run and the device->host read of the
+best tree inside the timed region).  `batched_mix` runs 512 uneven
+datasets in one batched launch against one plain launch per dataset.
 
 --impl reference runs the reference's CPU implementation of the path
-(the C restatement in oracle/, threaded over chains) on the same workload.
+(the C restatement in oracle/, threaded over chains) on the same data.
 N > 1: one process per GPU, independent replicas (no data-path collective).
 """
 from __future__ import annotations
@@ -69,7 +74,10 @@ def parse_args(argv=None):
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--autotune-steps", type=int, default=200)
     ap.add_argument("--launch", default="",
-                    help="cells_per_lane,warps_per_chain,chains_per_block")
+                    help="plain form: cells_per_lane,warps_per_chain,"
+                         "chains_per_block")
+    ap.add_argument("--mix-datasets", type=int, default=512)
+    ap.add_argument("--mix-steps", type=int, default=1000)
     return ap.parse_args(argv)
 
 
@@ -234,6 +242,75 @@ def _traffic_from_profile():
     return d.get("dram_bytes_per_chain_per_launch")
 
 
+def _timed(run, last_ms, steps, flush, barrier, torch):
+    """Runs `steps` launches between barriers and device syncs; returns
+    (sum of per-launch device ms, wall seconds, per-launch ms)."""
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ms = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        run()
+        ms.append(last_ms())
+    torch.cuda.synchronize()
+    barrier()
+    return sum(ms), time.perf_counter() - t0, ms
+
+
+def mix_datasets(n_datasets: int, seed: int = 512):
+    """The uneven mix: genes U[16,127], cells U[16,256], alpha log-uniform
+    in [1e-5, 1e-2], beta U[0.05, 0.45], unknown U[0, 0.15]."""
+    import numpy as np
+
+    from bbscite_gb300 import data as D
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_datasets):
+        G = int(rng.integers(16, 128))
+        Cn = int(rng.integers(16, 257))
+        a = float(10 ** rng.uniform(-5, -2))
+        b = float(rng.uniform(0.05, 0.45))
+        u = float(rng.uniform(0.0, 0.15))
+        m, _, _ = D.generate_dataset(seed * 1000 + i, G, Cn, a, b, u, 0.0)
+        mut, known = D.matrix_to_bits(m)
+        out.append(((mut, known, Cn, G), a, b))
+    return out
+
+
+def run_mix(N, n_datasets, chains, steps, flush, torch):
+    """Batched launch (autotuned, CUDA graph) vs one plain launch per
+    dataset, device time of the runs only."""
+    mix = mix_datasets(n_datasets)
+    params = [N.default_params(alpha_mean=a, beta_mean=b, seed=900 + i)
+              for i, (_, a, b) in enumerate(mix)]
+    with N.Batch([d for d, _, _ in mix], params) as bt:
+        bt.init_chains(chains)
+        bt.autotune(max(16, steps // 10))
+        bt.run(steps)
+        flush.zero_()
+        torch.cuda.synchronize()
+        bt.run(steps)
+        batched_ms = bt.last_run_ms()
+        shape = bt.launch()
+    seq_ms = 0.0
+    for i, ((mut, known, Cn, G), _, _) in enumerate(mix):
+        with N.Context(mut, known, Cn, G, params[i]) as c:
+            c.init_chains(chains)
+            c.run(steps)
+            seq_ms += c.last_run_ms()
+    total = n_datasets * chains * steps
+    return {"datasets": n_datasets, "chains_per_dataset": chains,
+            "steps": steps,
+            "batched_chain_steps_per_s": total / (batched_ms / 1e3),
+            "sequential_chain_steps_per_s": total / (seq_ms / 1e3),
+            "speedup": seq_ms / batched_ms,
+            "batched_launch": {"cells_per_lane": shape[0],
+                               "warps_per_block": shape[1],
+                               "merged_row_widths": bool(shape[2])}}
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -257,88 +334,121 @@ def run_ours(args) -> None:
     G, Cn, chains, L = w["n_genes"], w["n_cells"], args.chains, \
         args.chain_steps
     _, mut, known = make_dataset(rank)
-    params = N.default_params(alpha_mean=w["alpha"], beta_mean=w["beta"],
-                              seed=0xB5C17E + rank)
-    ctx = N.Context(mut, known, Cn, G, params)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    # batched+adjoint: sum score, Langevin error move learning (alpha,
+    # beta) from the wrong start 1e-2 / 0.3, error-move probability 0.1
+    adj = N.default_params(alpha_mean=1e-2, beta_mean=0.3,
+                           seed=0xB5C17E + rank, prob_beta_change=0.1,
+                           score_mode=N.SCORE_SUM,
+                           error_move=N.ERROR_LANGEVIN)
+    # plain: the reference's max score, fixed rates at the generator's
+    plain = N.default_params(alpha_mean=w["alpha"], beta_mean=w["beta"],
+                             seed=0xB5C17E + rank)
+
+    bt = N.Batch([(mut, known, Cn, G)], adj)
+    bt.init_chains(chains)
+    if args.autotune:
+        bt.autotune(args.autotune_steps)
+    bshape = bt.launch()
+    ctx = N.Context(mut, known, Cn, G, plain)
     ctx.init_chains(chains)
-    # launch shape from the autotuner (chain state is restored afterwards)
     if args.launch:
         ctx.set_launch(*[int(x) for x in args.launch.split(",")])
     elif args.autotune:
         ctx.autotune(args.autotune_steps)
-    shape = ctx.launch()
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
+    pshape = ctx.launch()
 
     for _ in range(args.warmup):
+        bt.run(L)
         ctx.run(L)
     clocks = ClockSampler(local)
-    barrier()
-    torch.cuda.synchronize()
     clocks.start()
-    t0 = time.perf_counter()
-    kernel_ms = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        ctx.run(L)
-        kernel_ms.append(ctx.last_run_ms())
-    torch.cuda.synchronize()
-    barrier()
-    wall = time.perf_counter() - t0
+    adj_ms, adj_wall, adj_list = _timed(lambda: bt.run(L), bt.last_run_ms,
+                                        args.steps, flush, barrier, torch)
+    pl_ms, pl_wall, pl_list = _timed(lambda: ctx.run(L), ctx.last_run_ms,
+                                     args.steps, flush, barrier, torch)
     clk = clocks.stop()
-    dev_s = sum(kernel_ms) / 1e3
     if dist is not None:
-        t = torch.tensor([dev_s, wall], device="cuda", dtype=torch.float64)
+        t = torch.tensor([adj_ms, adj_wall, pl_ms, pl_wall], device="cuda",
+                         dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, wall = float(t[0]), float(t[1])
-    total_steps = ws * chains * L * args.steps
-    value = total_steps / dev_s
-    best = ctx.best()
+        adj_ms, adj_wall, pl_ms, pl_wall = (float(x) for x in t)
+    steps_total = ws * chains * L * args.steps
+    value = steps_total / (adj_ms / 1e3)
+    plain_value = steps_total / (pl_ms / 1e3)
+
+    # equal best logL: both best trees under the reference's max score at
+    # the generator's rates (alpha=1e-3, beta=0.2)
+    ab = bt.best(0)
+    pb = ctx.best()
+    s_adj, _, _ = ctx.score_trees(ab["dm"][None], w["beta"])
+    s_pl, _, _ = ctx.score_trees(pb["dm"][None], w["beta"])
+    bt.close()
     ctx.close()
 
-    # roofline of the chain kernel (integer pipe: POPC)
+    # roofline of the headline kernel (integer pipe: POPC)
     popc_step = popc_per_chain_step(G, Cn)
-    launch_s = statistics.mean(kernel_ms) / 1e3
-    achieved = popc_step * chains * L / launch_s
+    achieved = popc_step * chains * L / (statistics.mean(adj_list) / 1e3)
     peak, clk_hz = N.popc_peak()
     traffic = _traffic_from_profile()
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers (batched+adjoint)
     e2e_times = []
-    h2d = d2h = 0
     for _ in range(args.e2e_steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        c2 = N.Context(mut, known, Cn, G, params)
-        parents = N.random_parents(params.seed, G, chains)
-        c2.init_chains(chains, parents)
-        c2.set_launch(*shape)
-        c2.run(L)
-        b2 = c2.best()
-        c2.close()
+        b2 = N.Batch([(mut, known, Cn, G)], adj)
+        b2.init_chains(chains)
+        b2.set_launch(*bshape)
+        b2.run(L)
+        b2.best(0)
+        b2.close()
         e2e_times.append(time.perf_counter() - t)
-        h2d = mut.nbytes + known.nbytes + chains * (G + 1) * N.words(G + 1) * 8
-        d2h = chains * 64 + (G + 1) * N.words(G + 1) * 8
-        del b2
+    W64 = N.words(G + 1)
+    h2d = mut.nbytes + known.nbytes + chains * (G + 1) * W64 * 8
+    d2h = 128 * chains + (G + 1) * W64 * 8
     e2e_value = ws * chains * L / statistics.mean(e2e_times)
+
+    mix = None
+    if rank == 0 and args.mix_datasets > 0:
+        mix = run_mix(N, args.mix_datasets, 32, args.mix_steps, flush, torch)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": wall * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32-popcount+f32",
+        "ms_per_step": adj_wall * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32-popcount+f32",
         "data": "synthetic (seeded generator, verification/lib.py semantics)",
-        "form": "plain persistent chain kernel (one warp per chain)",
+        "form": "batched+adjoint: work-list launch, sum-over-attachments "
+                "score with its fused adjoint, Langevin error-rate move",
         "config": {
-            "workload": f"{G} genes x {Cn} cells, {chains} chains, plain MCMC,"
-                        " fixed error rates alpha=1e-3 beta=0.2, Philox moves",
+            "workload": f"{G} genes x {Cn} cells, {chains} chains; data "
+                        "alpha=1e-3 beta=0.2 (10% unknown, 2% homozygous); "
+                        "chains learn alpha, beta from 1e-2, 0.3 (error move "
+                        "probability 0.1)",
             "n_genes": G, "n_cells": Cn, "chains": chains,
             "chain_steps_per_launch": L, "parallelism": f"replicas x{ws}",
-            "launch": {"cells_per_lane": shape[0],
-                       "warps_per_chain": shape[1],
-                       "chains_per_block": shape[2],
+            "launch": {"cells_per_lane": bshape[0],
+                       "warps_per_block": bshape[1],
                        "autotuned": bool(args.autotune)},
             "l2": "256 MiB buffer written between launches",
+        },
+        "plain": {
+            "value": plain_value, "unit": UNIT,
+            "form": "one-dataset persistent kernel, reference max score, "
+                    "fixed alpha=1e-3 beta=0.2",
+            "launch": {"cells_per_lane": pshape[0],
+                       "warps_per_chain": pshape[1],
+                       "chains_per_block": pshape[2]},
+            "ms_per_step": pl_wall * 1e3 / args.steps,
+        },
+        "equal_best_logl": {
+            "scored_with": "reference max score at alpha=1e-3 beta=0.2",
+            "batched_adjoint": float(s_adj[0]), "plain": float(s_pl[0]),
+            "difference": float(s_adj[0] - s_pl[0]),
+            "within_0.1_nats": bool(s_adj[0] >= s_pl[0] - 0.1),
+            "learned_alpha": ab["alpha"], "learned_beta": ab["beta"],
         },
         "roofline": {
             "bound": "int (POPC pipe)", "achieved": achieved / 1e9,
@@ -350,15 +460,18 @@ def run_ours(args) -> None:
             "peak_source": "bbs_popc_peak microbenchmark on this GPU "
                            f"(SM clock {clk_hz / 1e6:.0f} MHz)",
             "work_per_chain_step": f"{popc_step} POPC (32-bit)",
+            "plain_frac": popc_step * chains * L /
+            (statistics.mean(pl_list) / 1e3) / peak,
         },
         "counted_tbit_per_s": value * counted_bits_per_chain_step(G, Cn)
         / 1e12,
-        "best_logl": best["score"],
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
+    if mix is not None:
+        out["batched_mix"] = mix
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         b = cpu_baseline(args.cpu_seconds)
         out["cpu_baseline"] = {k: b[k] for k in

@@ -117,7 +117,9 @@ typedef struct bbs_step_trace {
   float proposed_beta;
   uint32_t accepted;
   float proposed_alpha;
-  uint32_t reserved[3];
+  float proposed_max_score; /* the reference's max score of the proposal
+                               (equal to proposed_score with that score) */
+  uint32_t reserved[2];
   uint64_t proposed_counts[4]; /* class totals n00,n01,n10,n11 (max score) */
 } bbs_step_trace;
 
@@ -215,7 +217,9 @@ BBS_API int bbs_last_run_ms(const bbs_ctx *ctx, float *ms);
 
 /* get_best_am/dm/beta/score, src/Application.hpp:224-256; also the parent
  * vector, the class totals (n00,n01,n10,n11) and the chain index.  Any
- * output pointer may be NULL. */
+ * output pointer may be NULL.  The best proposal is judged by the
+ * reference's max score also when chains sample the sum score (whose
+ * class totals are then not recorded: counts are zero). */
 BBS_API int bbs_get_best(bbs_ctx *ctx, uint64_t *am, uint64_t *dm, uint32_t *parent,
                  float *beta, float *score, uint64_t *counts,
                  uint32_t *chain);
@@ -268,7 +272,8 @@ BBS_API int bbs_batch_init_chains(bbs_batch *batch, uint32_t chains_per_dataset)
  * graph captured on the first run with this n_steps. */
 BBS_API int bbs_batch_run(bbs_batch *batch, uint32_t n_steps);
 BBS_API int bbs_batch_last_run_ms(const bbs_batch *batch, float *ms);
-/* Launch shape: cells per lane (1, 2 or 4) and warps per block (1-4);
+/* Launch shape: cells per lane (1-4; 1-2 above 128 nodes) and warps per
+ * block (1-4);
  * merge_rows != 0 runs 1- and 3-word trees with their 2- and 4-word row
  * stride group (one launch per group instead of two). */
 BBS_API int bbs_batch_set_launch(bbs_batch *batch, int cells_per_lane,

@@ -105,6 +105,11 @@ def replay(orc, native, m, p, start, trace, final_dm):
                 assert abs(logit(float(pb)) - eb) < 2e-3 * max(1, abs(eb))
         S1, e1 = evaluate(ndm, pa, pb)
         assert abs(t["proposed_score"] - S1) <= SCORE_RTOL * abs(S1) + 1e-4
+        smax, _ = orc.score_counts_f64(float(pa), float(pb), ndm, mut, known,
+                                       False)
+        smax += orc.logprior_beta_f64(float(p.beta_mean), float(p.beta_sd),
+                                      float(pb))
+        assert abs(t["proposed_max_score"] - smax) <= SCORE_RTOL * abs(smax) + 1e-4
         geo1 = geometry(float(pa), float(pb), e1, gamma, A, B)
         if raw["move_type"] == 0 and p.error_move != native.ERROR_BETA_WALK:
             fa, fb = logit(float(alpha)), logit(float(beta))
