@@ -60,7 +60,8 @@ def elf_matches_host(path: str) -> bool:
 
 def _deps() -> float:
     files = glob.glob(os.path.join(CSRC, "*")) + [
-        os.path.join(INCLUDE, "bbscite_gb300.h")]
+        os.path.join(INCLUDE, "bbscite_gb300.h"),
+        os.path.join(INCLUDE, "bbscite_gb300.hpp")]
     return max(os.path.getmtime(f) for f in files)
 
 

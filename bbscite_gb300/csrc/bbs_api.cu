@@ -1076,6 +1076,13 @@ int bbs_score_trees(bbs_ctx *c, const uint64_t *dm, const float *betas,
   }
 }
 
+int bbs_logscore_beta(const bbs_ctx *c, float beta, float *out) {
+  if (!c || !out) return fail(BBS_ERR_INPUT, "NULL argument");
+  float l01, l11;
+  host_beta_terms(c->ds, beta, &l01, &l11, out);
+  return BBS_OK;
+}
+
 int bbs_apply_moves(bbs_ctx *c, const uint64_t *dm, const float *betas,
                     uint32_t n_trees, const bbs_raw_move *raw,
                     const bbs_move_params *params,

@@ -71,6 +71,9 @@ def parse_args(argv=None):
                     help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--quality-steps", type=int, default=200000,
+                    help="untimed steps per chain of both forms before the "
+                         "warm-up (the equal-best-logL comparison)")
     ap.add_argument("--autotune", type=int, default=1)
     ap.add_argument("--autotune-steps", type=int, default=200)
     ap.add_argument("--launch", default="",
@@ -78,6 +81,14 @@ def parse_args(argv=None):
                          "chains_per_block")
     ap.add_argument("--mix-datasets", type=int, default=512)
     ap.add_argument("--mix-steps", type=int, default=1000)
+    ap.add_argument("--lvr-steps", type=int, default=500000,
+                    help="Langevin vs random walk: steps per chain (0: off)")
+    ap.add_argument("--lvr-seeds", type=int, default=4)
+    ap.add_argument("--lvr-chains", type=int, default=256)
+    ap.add_argument("--lvr-error-step", type=float, default=1.2)
+    ap.add_argument("--caps-steps", type=int, default=200,
+                    help="255x512 run: steps per launch (0: off)")
+    ap.add_argument("--caps-chains", type=int, default=4096)
     return ap.parse_args(argv)
 
 
@@ -281,7 +292,10 @@ def mix_datasets(n_datasets: int, seed: int = 512):
 
 def run_mix(N, n_datasets, chains, steps, flush, torch):
     """Batched launch (autotuned, CUDA graph) vs one plain launch per
-    dataset, device time of the runs only."""
+    dataset, device time of the runs only.  The plain form runs each chain
+    on one warp (cells_per_lane = min(ceil(C/32), 4), one chain per block);
+    the tuned single-dataset form lets each launch spread a chain's cells
+    over up to 4 warps (the context's default launch heuristic)."""
     mix = mix_datasets(n_datasets)
     params = [N.default_params(alpha_mean=a, beta_mean=b, seed=900 + i)
               for i, (_, a, b) in enumerate(mix)]
@@ -294,21 +308,165 @@ def run_mix(N, n_datasets, chains, steps, flush, torch):
         bt.run(steps)
         batched_ms = bt.last_run_ms()
         shape = bt.launch()
-    seq_ms = 0.0
+    plain_ms = tuned_ms = 0.0
     for i, ((mut, known, Cn, G), _, _) in enumerate(mix):
         with N.Context(mut, known, Cn, G, params[i]) as c:
             c.init_chains(chains)
             c.run(steps)
-            seq_ms += c.last_run_ms()
+            tuned_ms += c.last_run_ms()
+            c.init_chains(chains)
+            c.set_launch(min((Cn + 31) // 32, 4), 1, 1)
+            c.run(steps)
+            plain_ms += c.last_run_ms()
     total = n_datasets * chains * steps
     return {"datasets": n_datasets, "chains_per_dataset": chains,
             "steps": steps,
             "batched_chain_steps_per_s": total / (batched_ms / 1e3),
-            "sequential_chain_steps_per_s": total / (seq_ms / 1e3),
-            "speedup": seq_ms / batched_ms,
+            "sequential_plain_chain_steps_per_s": total / (plain_ms / 1e3),
+            "speedup": plain_ms / batched_ms,
+            "sequential_tuned_chain_steps_per_s": total / (tuned_ms / 1e3),
+            "speedup_vs_tuned_single": tuned_ms / batched_ms,
+            "pairs_per_chain_step": mix_pairs(mix),
             "batched_launch": {"cells_per_lane": shape[0],
                                "warps_per_block": shape[1],
                                "merged_row_widths": bool(shape[2])}}
+
+
+def mix_pairs(mix) -> float:
+    """Mean (cell, node) pairs scored per chain-step over the mix."""
+    return sum(Cn * (G + 1) for (_, _, Cn, G), _, _ in mix) / len(mix)
+
+
+def _logit(x):
+    return math.log(x / (1.0 - x))
+
+
+def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
+                       error_step, data_alpha, data_beta):
+    """Steps-to-best of the adjoint-driven Langevin error-rate chain (sum
+    score) against the random-walk error-rate chain (the reference's max
+    score), both from alpha=1e-2, beta=0.3 with error-move probability 0.1,
+    over `seeds` independent seeds (the same Philox seeds in both arms).
+    At every checkpoint (1,000-step chunks to 20,000 steps, then
+    10,000-step chunks) each arm's best tree is scored with the reference's
+    max score at the generator's rates (a scale common to both arms: the
+    chains judge proposals at their own sampled rates), and the median over
+    chains of logit(alpha) and logit(beta) is read.  Per seed: the first
+    step count at which the Langevin arm's best is within 0.1 nats of the
+    random-walk arm's final best, and for each arm the step count after
+    which the median rates stay within 0.25 (logit alpha) and 0.05 (logit
+    beta) of their final values."""
+    import numpy as np
+
+    arms = {"random_walk": (N.SCORE_MAX, N.ERROR_RANDOM_WALK),
+            "langevin": (N.SCORE_SUM, N.ERROR_LANGEVIN)}
+    marks = list(range(1000, 20001, 1000)) + \
+        list(range(30000, total + 1, 10000))
+    res = {a: [] for a in arms}
+    sp = N.default_params(alpha_mean=data_alpha, beta_mean=data_beta)
+    with N.Context(mut, known, Cn, G, sp) as scorer:
+        for sd in range(seeds):
+            for name, (mode, move) in arms.items():
+                p = N.default_params(alpha_mean=1e-2, beta_mean=0.3,
+                                     seed=0x1A6E + 7919 * sd,
+                                     prob_beta_change=0.1, score_mode=mode,
+                                     error_move=move, error_step=error_step)
+                with N.Context(mut, known, Cn, G, p) as c:
+                    c.init_chains(chains)
+                    best, own, la, lb, done = [], [], [], [], 0
+                    for mk in marks:
+                        c.run(mk - done)
+                        done = mk
+                        b = c.best()
+                        own.append(float(b["score"]))
+                        best.append(float(scorer.score_trees(
+                            b["dm"][None], data_beta)[0][0]))
+                        st = c.chains()
+                        la.append(float(np.median([_logit(x) for x in
+                                                   st["alpha"]])))
+                        lb.append(float(np.median([_logit(x) for x in
+                                                   st["beta"]])))
+                    e = c.chains()["err_stats"].sum(axis=0)
+                settle = 0
+                for k in range(len(marks)):
+                    if abs(la[k] - la[-1]) > 0.25 or \
+                            abs(lb[k] - lb[-1]) > 0.05:
+                        settle = marks[k]
+                res[name].append({"best": best, "own": own[-1],
+                                  "settle": settle,
+                                  "accept": float(e[1]) / max(1, int(e[0]))})
+    per_seed = []
+    for sd in range(seeds):
+        target = res["random_walk"][sd]["best"][-1] - 0.1
+        reach = {a: next((marks[k] for k, v in enumerate(res[a][sd]["best"])
+                          if v >= target), None) for a in arms}
+        per_seed.append({
+            "random_walk_best": res["random_walk"][sd]["best"][-1],
+            "langevin_best": res["langevin"][sd]["best"][-1],
+            "random_walk_steps_to_own_best": reach["random_walk"],
+            "langevin_steps_to_rw_best": reach["langevin"],
+            "best_at_own_rates": {a: res[a][sd]["own"] for a in arms}})
+    ratios = sorted(p["langevin_steps_to_rw_best"] /
+                    p["random_walk_steps_to_own_best"]
+                    if p["langevin_steps_to_rw_best"] is not None else math.inf
+                    for p in per_seed)
+    med = ratios[len(ratios) // 2] if seeds % 2 else \
+        0.5 * (ratios[seeds // 2 - 1] + ratios[seeds // 2])
+    return {
+        "chains": chains, "steps": total, "seeds": seeds,
+        "error_step": error_step, "n_genes": G, "n_cells": Cn,
+        "scored_with": f"reference max score at alpha={data_alpha:g} "
+                       f"beta={data_beta:g}",
+        "per_seed": per_seed,
+        "median_step_ratio_langevin_over_rw": med,
+        "target_half_met": med <= 0.5,
+        "rates_settle_steps": {a: [r["settle"] for r in res[a]] for a in arms},
+        "error_move_acceptance": {a: [round(r["accept"], 3) for r in res[a]]
+                                  for a in arms},
+    }
+
+
+def run_beyond_caps(N, chains, steps, flush, torch):
+    """255 genes x 512 cells (alpha=5e-4, beta=0.25, 8% unknown, 1%
+    homozygous): the batched form with the sum score and Langevin error
+    moves against the plain form (max score, fixed rates), device time of
+    one launch of `steps` steps after a warm-up launch."""
+    from bbscite_gb300 import data as D
+    G, Cn = 255, 512
+    m, _, _ = D.generate_dataset(5255, G, Cn, 5e-4, 0.25, 0.08, 0.01)
+    mut, known = D.matrix_to_bits(m)
+    adj = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5,
+                           prob_beta_change=0.1, score_mode=N.SCORE_SUM,
+                           error_move=N.ERROR_LANGEVIN)
+    plain = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5)
+    out = {"n_genes": G, "n_cells": Cn, "chains": chains, "steps": steps}
+    with N.Batch([(mut, known, Cn, G)], adj) as bt:
+        bt.init_chains(chains)
+        bt.autotune(max(8, steps // 10))
+        bt.run(steps)
+        flush.zero_()
+        torch.cuda.synchronize()
+        bt.run(steps)
+        out["batched_adjoint_chain_steps_per_s"] = \
+            chains * steps / (bt.last_run_ms() / 1e3)
+        out["batched_launch"] = list(bt.launch())
+    with N.Context(mut, known, Cn, G, plain) as c:
+        c.init_chains(chains)
+        c.autotune(max(8, steps // 10))
+        c.run(steps)
+        flush.zero_()
+        torch.cuda.synchronize()
+        c.run(steps)
+        out["plain_chain_steps_per_s"] = \
+            chains * steps / (c.last_run_ms() / 1e3)
+        out["plain_launch"] = list(c.launch())
+    popc = popc_per_chain_step(G, Cn)
+    peak, _ = N.popc_peak()
+    out["popc_per_chain_step"] = popc
+    out["batched_adjoint_frac"] = \
+        out["batched_adjoint_chain_steps_per_s"] * popc / peak
+    out["plain_frac"] = out["plain_chain_steps_per_s"] * popc / peak
+    return out
 
 
 def run_ours(args) -> None:
@@ -358,6 +516,12 @@ def run_ours(args) -> None:
         ctx.autotune(args.autotune_steps)
     pshape = ctx.launch()
 
+    done = 0
+    while done < args.quality_steps:
+        k = min(L, args.quality_steps - done)
+        bt.run(k)
+        ctx.run(k)
+        done += k
     for _ in range(args.warmup):
         bt.run(L)
         ctx.run(L)
@@ -409,9 +573,16 @@ def run_ours(args) -> None:
     d2h = 128 * chains + (G + 1) * W64 * 8
     e2e_value = ws * chains * L / statistics.mean(e2e_times)
 
-    mix = None
+    mix = lvr = caps = None
     if rank == 0 and args.mix_datasets > 0:
         mix = run_mix(N, args.mix_datasets, 32, args.mix_steps, flush, torch)
+    if rank == 0 and args.lvr_steps > 0:
+        lvr = run_langevin_vs_rw(N, mut, known, G, Cn, args.lvr_chains,
+                                 args.lvr_steps, args.lvr_seeds,
+                                 args.lvr_error_step, w["alpha"], w["beta"])
+    if rank == 0 and args.caps_steps > 0:
+        caps = run_beyond_caps(N, args.caps_chains, args.caps_steps, flush,
+                               torch)
 
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
@@ -445,6 +616,8 @@ def run_ours(args) -> None:
         },
         "equal_best_logl": {
             "scored_with": "reference max score at alpha=1e-3 beta=0.2",
+            "steps_per_chain": args.quality_steps
+            + (args.warmup + args.steps) * L,
             "batched_adjoint": float(s_adj[0]), "plain": float(s_pl[0]),
             "difference": float(s_adj[0] - s_pl[0]),
             "within_0.1_nats": bool(s_adj[0] >= s_pl[0] - 0.1),
@@ -472,6 +645,10 @@ def run_ours(args) -> None:
     }
     if mix is not None:
         out["batched_mix"] = mix
+    if lvr is not None:
+        out["langevin_vs_random_walk"] = lvr
+    if caps is not None:
+        out["beyond_caps_255x512"] = caps
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         b = cpu_baseline(args.cpu_seconds)
         out["cpu_baseline"] = {k: b[k] for k in

@@ -241,6 +241,12 @@ BBS_API int bbs_score_trees(bbs_ctx *ctx, const uint64_t *dm, const float *betas
                     uint32_t n_trees, float *scores, uint64_t *counts,
                     uint32_t *attach);
 
+/* TreeScorer::logscore_beta, src/TreeScorer.hpp:122-126: the log Beta
+ * prior of `beta` with the context's (beta_mean, beta_sd), in FP32 through
+ * log(tgamma(.)) as the reference computes it (NaN where tgammaf
+ * overflows, a + b above about 35). */
+BBS_API int bbs_logscore_beta(const bbs_ctx *ctx, float beta, float *out);
+
 /* realize_raw_move_sample + update constructor for a batch,
  * src/MutationTree.hpp:123-363.  When `raw` is non-NULL each move is
  * realised first (params_out, optional, receives the result); otherwise

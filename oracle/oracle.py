@@ -212,6 +212,14 @@ def n_ancestors(dm, x: int) -> int:
                                          C.c_uint32(x)))
 
 
+def descendant_or_nondescendant(am, x: int, k: int, descendant: bool) -> int:
+    """src/MutationTree.hpp:840-878: the k-th descendant (or non-descendant)
+    of x, 0 when k is out of range."""
+    return int(lib().orc_get_descendant_or_nondescendant(
+        _p(am), C.c_uint32(am.shape[0]), C.c_uint32(x), C.c_uint32(k),
+        C.c_int(1 if descendant else 0)))
+
+
 def realize(am, dm, beta: float, raw) -> np.ndarray:
     out = np.zeros(1, dtype=MOD_PARAMS)
     raw = np.ascontiguousarray(np.asarray(raw, dtype=RAW_MOVE).reshape(1))
