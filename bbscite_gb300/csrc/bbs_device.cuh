@@ -599,8 +599,29 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     mx[q] = -INFINITY;
     z[q] = ed[q] = em[q] = 0.0f;
   }
+  // two nodes per iteration: independent work for the scheduler
+  int j = 0;
 #pragma unroll 1
-  for (int j = 0; j < n; j++) {
+  for (; j + 1 < n; j += 2) {
+    uint32_t a[W32], b[W32];
+    ld_row<W32>(rows + j * RS, a);
+    ld_row<W32>(rows + (j + 1) * RS, b);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const float fd0 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+      const float fm0 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+      const float fd1 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
+      const float fm1 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
+      const float t0 = fmaf(fd0, c1, fmaf(fm0, c2, base[q]));
+      const float t1 = fmaf(fd1, c1, fmaf(fm1, c2, base[q]));
+      const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
+      mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
+      z[q] += e0 + e1;
+      ed[q] = fmaf(e0, fd0, fmaf(e1, fd1, ed[q]));
+      em[q] = fmaf(e0, fm0, fmaf(e1, fm1, em[q]));
+    }
+  }
+  if (j < n) {
     uint32_t a[W32];
     ld_row<W32>(rows + j * RS, a);
 #pragma unroll

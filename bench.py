@@ -79,6 +79,9 @@ def parse_args(argv=None):
     ap.add_argument("--launch", default="",
                     help="plain form: cells_per_lane,warps_per_chain,"
                          "chains_per_block")
+    ap.add_argument("--batch-launch", default="",
+                    help="batched form: cells_per_lane,warps_per_block,"
+                         "merge_rows")
     ap.add_argument("--mix-datasets", type=int, default=512)
     ap.add_argument("--mix-steps", type=int, default=1000)
     ap.add_argument("--lvr-steps", type=int, default=500000,
@@ -359,7 +362,8 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     import numpy as np
 
     arms = {"random_walk": (N.SCORE_MAX, N.ERROR_RANDOM_WALK),
-            "langevin": (N.SCORE_SUM, N.ERROR_LANGEVIN)}
+            "langevin": (N.SCORE_SUM, N.ERROR_LANGEVIN),
+            "langevin_max_score": (N.SCORE_MAX, N.ERROR_LANGEVIN)}
     marks = list(range(1000, 20001, 1000)) + \
         list(range(30000, total + 1, 10000))
     res = {a: [] for a in arms}
@@ -401,25 +405,29 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
         reach = {a: next((marks[k] for k, v in enumerate(res[a][sd]["best"])
                           if v >= target), None) for a in arms}
         per_seed.append({
-            "random_walk_best": res["random_walk"][sd]["best"][-1],
-            "langevin_best": res["langevin"][sd]["best"][-1],
-            "random_walk_steps_to_own_best": reach["random_walk"],
-            "langevin_steps_to_rw_best": reach["langevin"],
+            "best": {a: res[a][sd]["best"][-1] for a in arms},
+            "steps_to_rw_best": reach,
             "best_at_own_rates": {a: res[a][sd]["own"] for a in arms}})
-    ratios = sorted(p["langevin_steps_to_rw_best"] /
-                    p["random_walk_steps_to_own_best"]
-                    if p["langevin_steps_to_rw_best"] is not None else math.inf
-                    for p in per_seed)
-    med = ratios[len(ratios) // 2] if seeds % 2 else \
-        0.5 * (ratios[seeds // 2 - 1] + ratios[seeds // 2])
+
+    def median_ratio(arm):
+        r = sorted(p["steps_to_rw_best"][arm] /
+                   p["steps_to_rw_best"]["random_walk"]
+                   if p["steps_to_rw_best"][arm] is not None else math.inf
+                   for p in per_seed)
+        return r[len(r) // 2] if seeds % 2 else \
+            0.5 * (r[seeds // 2 - 1] + r[seeds // 2])
+    ratios = {a: median_ratio(a) for a in arms if a != "random_walk"}
     return {
         "chains": chains, "steps": total, "seeds": seeds,
         "error_step": error_step, "n_genes": G, "n_cells": Cn,
         "scored_with": f"reference max score at alpha={data_alpha:g} "
                        f"beta={data_beta:g}",
+        "arms": {a: {"score": "sum" if m == N.SCORE_SUM else "max",
+                     "error_move": "langevin" if e == N.ERROR_LANGEVIN
+                     else "random_walk"} for a, (m, e) in arms.items()},
         "per_seed": per_seed,
-        "median_step_ratio_langevin_over_rw": med,
-        "target_half_met": med <= 0.5,
+        "median_step_ratio_over_rw": ratios,
+        "target_half_met": ratios["langevin"] <= 0.5,
         "rates_settle_steps": {a: [r["settle"] for r in res[a]] for a in arms},
         "error_move_acceptance": {a: [round(r["accept"], 3) for r in res[a]]
                                   for a in arms},
@@ -505,7 +513,9 @@ def run_ours(args) -> None:
 
     bt = N.Batch([(mut, known, Cn, G)], adj)
     bt.init_chains(chains)
-    if args.autotune:
+    if args.batch_launch:
+        bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
+    elif args.autotune:
         bt.autotune(args.autotune_steps)
     bshape = bt.launch()
     ctx = N.Context(mut, known, Cn, G, plain)
@@ -602,7 +612,7 @@ def run_ours(args) -> None:
             "chain_steps_per_launch": L, "parallelism": f"replicas x{ws}",
             "launch": {"cells_per_lane": bshape[0],
                        "warps_per_block": bshape[1],
-                       "autotuned": bool(args.autotune)},
+                       "autotuned": bool(args.autotune) and not args.batch_launch},
             "l2": "256 MiB buffer written between launches",
         },
         "plain": {
