@@ -245,10 +245,10 @@ def run_reference(args) -> None:
 
 # ------------------------------------------------------------------ ours --
 
-def _traffic_from_profile():
-    """DRAM bytes per launch of the chain kernel from the committed ncu
-    summary (profiles/mcmc_95x96_dram.json), or None."""
-    p = os.path.join(ROOT, "profiles", "mcmc_95x96_dram.json")
+def _traffic_from_profile(name="batch_95x96_dram.json"):
+    """DRAM bytes per chain per launch of a chain kernel from the committed
+    ncu summary under profiles/, or None."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     with open(p) as f:
@@ -639,7 +639,7 @@ def run_ours(args) -> None:
             "frac": achieved / peak,
             "traffic": (traffic * chains) if traffic is not None else None,
             "traffic_unit": "bytes per launch (ncu dram read+write, "
-                            "profiles/mcmc_95x96_dram.json)",
+                            "profiles/batch_95x96_dram.json)",
             "peak_source": "bbs_popc_peak microbenchmark on this GPU "
                            f"(SM clock {clk_hz / 1e6:.0f} MHz)",
             "work_per_chain_step": f"{popc_step} POPC (32-bit)",
