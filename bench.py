@@ -212,6 +212,52 @@ def cpu_baseline(seconds: float, rank: int = 0) -> dict:
             "best_logl": best}
 
 
+def cpu_scoring_proxy_rate(seconds: float) -> dict:
+    """The reference's CPU scoring benchmark restated
+    (cpu_scoring_benchmark/CPUTreeScorer.hpp:97-213 at its fixed 128 cells
+    x 127 genes): repeated scorings of fixed random trees on all host
+    cores, as scorings/s and the paper's counted bits (4 * 128 * 128^2 per
+    scoring; Table 4 quotes 233.05 k scorings/s and 1.95 Tbit/s on two Xeon
+    Gold 6148)."""
+    import numpy as np
+
+    from bbscite_gb300 import data as D
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    m, _, _ = D.generate_dataset(128127, 127, 128, 1e-3, 0.2, 0.05, 0.0)
+    # [quadword][gene] words with one bit per cell (128 cells, 128 slots)
+    mutq = np.zeros((2, 128), dtype=np.uint64)
+    knownq = np.zeros((2, 128), dtype=np.uint64)
+    for g in range(127):
+        for c in range(128):
+            b = np.uint64(1) << np.uint64(c % 64)
+            if m[g, c] != 3:
+                knownq[c // 64, g] |= b
+            if m[g, c] in (1, 2):
+                mutq[c // 64, g] |= b
+    # per tree [quadword][node] ancestor words
+    rng = np.random.default_rng(128)
+    trees = [np.ascontiguousarray(O.parent_to_matrix(
+        D.random_parent_vector(rng, 127))[1].T) for _ in range(32)]
+    n_trees = 64 * threads
+    dmq = np.ascontiguousarray(np.stack([trees[t % 32]
+                                         for t in range(n_trees)]))
+    t0 = time.perf_counter()
+    O.cpu_scoring_proxy(1e-3, 0.2, mutq, knownq, dmq, n_trees, 4, threads)
+    rate = n_trees * 4 / (time.perf_counter() - t0)
+    reps = max(4, int(rate * seconds / n_trees))
+    t0 = time.perf_counter()
+    O.cpu_scoring_proxy(1e-3, 0.2, mutq, knownq, dmq, n_trees, reps, threads)
+    dt = time.perf_counter() - t0
+    per_s = n_trees * reps / dt
+    return {"scorings_per_s": per_s,
+            "counted_tbit_per_s": per_s * 4 * 128 * 128 ** 2 / 1e12,
+            "cores": threads, "kind": "port",
+            "sample": f"{n_trees * reps} scorings at 128 cells x 127 genes "
+                      f"({dt:.1f} s), oracle/bbs_oracle.c "
+                      "orc_cpu_scoring_proxy"}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -254,6 +300,37 @@ def _traffic_from_profile(name="batch_95x96_dram.json"):
     with open(p) as f:
         d = json.load(f)
     return d.get("dram_bytes_per_chain_per_launch")
+
+
+def max_over_ranks(dist, values, device):
+    """Each timing maximised over the ranks: the job's clock is its slowest
+    replica."""
+    import torch
+    if dist is None:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64,
+                     device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def global_best(dist, score, rank, world, device):
+    """The best score over the replicas and the rank holding it (the lowest
+    rank on ties): the one cross-replica step of the path, the final argmax
+    of src/Application.hpp:470-487 over independent chain sets."""
+    import torch
+    if dist is None:
+        return float(score), rank
+    mine = torch.tensor([float(score), float(rank)], dtype=torch.float64,
+                        device=device)
+    parts = [torch.zeros_like(mine) for _ in range(world)]
+    dist.all_gather(parts, mine)
+    best, who = None, None
+    for p in parts:
+        s, r = float(p[0]), int(p[1])
+        if best is None or s > best:
+            best, who = s, r
+    return best, who
 
 
 def _timed(run, last_ms, steps, flush, barrier, torch):
@@ -499,7 +576,7 @@ def run_ours(args) -> None:
     w = WORKLOAD
     G, Cn, chains, L = w["n_genes"], w["n_cells"], args.chains, \
         args.chain_steps
-    _, mut, known = make_dataset(rank)
+    _, mut, known = make_dataset()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device="cuda")
     # batched+adjoint: sum score, Langevin error move learning (alpha,
     # beta) from the wrong start 1e-2 / 0.3, error-move probability 0.1
@@ -542,11 +619,8 @@ def run_ours(args) -> None:
     pl_ms, pl_wall, pl_list = _timed(lambda: ctx.run(L), ctx.last_run_ms,
                                      args.steps, flush, barrier, torch)
     clk = clocks.stop()
-    if dist is not None:
-        t = torch.tensor([adj_ms, adj_wall, pl_ms, pl_wall], device="cuda",
-                         dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        adj_ms, adj_wall, pl_ms, pl_wall = (float(x) for x in t)
+    adj_ms, adj_wall, pl_ms, pl_wall = max_over_ranks(
+        dist, [adj_ms, adj_wall, pl_ms, pl_wall], "cuda")
     steps_total = ws * chains * L * args.steps
     value = steps_total / (adj_ms / 1e3)
     plain_value = steps_total / (pl_ms / 1e3)
@@ -559,6 +633,9 @@ def run_ours(args) -> None:
     s_pl, _, _ = ctx.score_trees(pb["dm"][None], w["beta"])
     bt.close()
     ctx.close()
+    # replicas share the dataset and differ in their seeds: best over ranks
+    s_adj = [global_best(dist, s_adj[0], rank, ws, "cuda")[0]]
+    s_pl = [global_best(dist, s_pl[0], rank, ws, "cuda")[0]]
 
     # roofline of the headline kernel (integer pipe: POPC)
     popc_step = popc_per_chain_step(G, Cn)
@@ -663,6 +740,8 @@ def run_ours(args) -> None:
         b = cpu_baseline(args.cpu_seconds)
         out["cpu_baseline"] = {k: b[k] for k in
                                ("value", "unit", "cores", "kind", "sample")}
+        out["cpu_baseline"]["scoring_proxy"] = cpu_scoring_proxy_rate(
+            min(5.0, args.cpu_seconds))
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:

@@ -15,6 +15,7 @@
 #include <TreeScorer.hpp>
 
 #include <cmath>
+#include <random>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -368,6 +369,42 @@ int ref_to_newick(const uint64_t *am, const uint64_t *dm, uint32_t n_nodes,
 // src/Parameters.hpp:61-281 on an argv; returns 1 if valid and fills
 // out[] = {alpha, beta, beta_sd, p_beta, p_prune, p_swap, p_subtrees,
 //          chi, gamma, n_chains, chain_length, max_treelist}.
+// One chain's initial tree and move stream from the reference's own
+// samplers and URNG: MutationTree::sample_random_pruefer_code
+// (src/MutationTree.hpp:492-510) decoded by pruefer_code_to_parent_vector,
+// RawMoveDistribution::operator() (src/RawMoveDistribution.hpp:97-155)
+// with the probabilities normalised by Parameters (src/Parameters.hpp:
+// 451-612), all drawn from std::minstd_rand (src/main.cpp:34) seeded with
+// `seed`.  The reference seeds one generator for all chains from
+// random_device; here each chain gets its own seed so runs repeat.
+void ref_sample_chain(uint32_t n_genes, float prob_beta_change,
+                      float prob_prune, float prob_swap, float prob_subtrees,
+                      float beta_sd, float chi, uint32_t seed,
+                      uint32_t n_steps, uint32_t *parent_out,
+                      void *moves_out) {
+  std::minstd_rand rng(seed);
+  const std::vector<uint32_t> code =
+      Tree<255>::sample_random_pruefer_code(rng, n_genes);
+  const std::vector<uint32_t> parent =
+      Tree<255>::pruefer_code_to_parent_vector(code);
+  std::memcpy(parent_out, parent.data(), sizeof(uint32_t) * parent.size());
+  Parameters p;
+  p.set_prob_beta_change(prob_beta_change);
+  p.set_prob_prune_n_reattach(prob_prune);
+  p.set_prob_swap_nodes(prob_swap);
+  p.set_prob_swap_subtrees(prob_subtrees);
+  p.set_beta_sd(beta_sd);
+  p.set_beta_jump_scaling_chi(chi);
+  RawMoveDistribution dist(n_genes + 1, p);
+  RawC *out = (RawC *)moves_out;
+  for (uint32_t i = 0; i < n_steps; i++) {
+    const RawMoveSample r = dist(rng);
+    out[i] = RawC{(int32_t)r.move_type, r.raw_v, r.raw_w,
+                  r.raw_descendant_of_v, r.raw_nondescendant_of_v,
+                  r.beta_jump, r.acceptance_level, 0u};
+  }
+}
+
 int ref_parse_args(int argc, char **argv, float *out) {
   Parameters p;
   bool ok = p.load_and_verify_args(argc, argv);

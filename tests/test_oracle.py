@@ -285,3 +285,25 @@ def test_sumscore_gradient_fd(orc):
         assert da == pytest.approx(fa, rel=1e-6)
         assert db == pytest.approx(fb, rel=1e-6)
         np.testing.assert_allclose(post.sum(axis=1), 1.0, rtol=1e-12)
+
+
+def test_quality_fixture_scores(orc):
+    """The committed reference results of the quality comparison are the
+    reference's cell-order scores of their best trees."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                        "quality_ref.json")
+    with open(path) as f:
+        fx = json.load(f)
+    w = fx["workload"]
+    assert len(fx["results"]) == w["datasets"] == 32
+    for row in fx["results"][:8]:
+        m, _, _ = D.generate_dataset(row["dataset_seed"], w["n_genes"],
+                                     w["n_cells"], w["alpha"], w["beta"],
+                                     w["missing"], w["homozygous"])
+        mut, known = D.matrix_to_bits(m)
+        _, dm = orc.parent_to_matrix(np.array(row["best_parent"]))
+        r, _, _, _ = orc.logscore_tree(w["alpha"], w["beta"], w["beta_sd"],
+                                       dm, mut, known, w["beta"])
+        assert np.float32(r) == np.float32(row["best_score"])
