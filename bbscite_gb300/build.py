@@ -32,7 +32,8 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off",
               "-Xcompiler", "-fvisibility=hidden", "-I" + INCLUDE,
               "-I" + CSRC]
-UNITS = ["bbs_mcmc_lo.cu", "bbs_mcmc_hi.cu", "bbs_aux.cu", "bbs_api.cu",
+UNITS = ["bbs_mcmc_lo.cu", "bbs_mcmc_lo_rec.cu", "bbs_mcmc_hi.cu",
+         "bbs_mcmc_hi_rec.cu", "bbs_aux.cu", "bbs_api.cu",
          "bbs_batch.cu"]
 
 

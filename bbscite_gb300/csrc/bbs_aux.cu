@@ -20,8 +20,12 @@ int launch_mcmc(const RunArgs &a, int q, int cpb, int n_sms, void *stream) {
   cudaStream_t s = (cudaStream_t)stream;
   const bool sum = a.md.score_mode == 1;
   if (w32 > 4) q = std::min(q, 2);
-  if (w32 <= 4) return launch_mcmc_lo(a, w32, q, sum, cpb, n_sms, s);
-  return launch_mcmc_hi(a, w32, q, sum, cpb, n_sms, s);
+  const bool rec = a.moves != nullptr || a.trace != nullptr;
+  if (w32 <= 4)
+    return rec ? launch_mcmc_lo_rec(a, w32, q, sum, cpb, n_sms, s)
+               : launch_mcmc_lo(a, w32, q, sum, cpb, n_sms, s);
+  return rec ? launch_mcmc_hi_rec(a, w32, q, sum, cpb, n_sms, s)
+             : launch_mcmc_hi(a, w32, q, sum, cpb, n_sms, s);
 }
 
 int launch_batch(const BatchArgs &b, int w32, int q, bool sum, int wpb,

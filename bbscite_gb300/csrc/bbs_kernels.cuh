@@ -303,8 +303,10 @@ struct McmcOccupancy {
 };
 
 // One dataset: chains 0..n_chains-1, one warp per chain (blocks of `cpb`
-// chains) or wpc warps per chain (the block is one chain).
-template <int W32, int Q, bool SUM>
+// chains) or wpc warps per chain (the block is one chain).  REC: recorded
+// moves and/or a step trace (replays and tests); without them the move and
+// trace paths compile away.
+template <int W32, int Q, bool SUM, bool REC>
 __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
     mcmc_kernel(const RunArgs a) {
   extern __shared__ __align__(16) uint32_t smem[];
@@ -325,11 +327,15 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
   for (int chain = blockIdx.x * cpb + slot; chain < a.n_chains;
        chain += gridDim.x * cpb) {
+    const bbs_raw_move *moves = nullptr;
+    bbs_step_trace *trace = nullptr;
+    if constexpr (REC) {
+      if (a.moves != nullptr) moves = a.moves + (size_t)chain * a.n_steps;
+      if (a.trace != nullptr) trace = a.trace + (size_t)chain * a.n_steps;
+    }
     run_chain<W32, Q, SUM>(
         a.ds, a.md, (uint32_t)chain, a.rows + (size_t)chain * n * RS,
-        a.best_rows + (size_t)chain * n * RS, a.states + chain,
-        a.moves != nullptr ? a.moves + (size_t)chain * a.n_steps : nullptr,
-        a.trace != nullptr ? a.trace + (size_t)chain * a.n_steps : nullptr,
+        a.best_rows + (size_t)chain * n * RS, a.states + chain, moves, trace,
         a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, cb, resident,
         wpc, wic, lane);
   }

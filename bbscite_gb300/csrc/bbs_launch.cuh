@@ -18,7 +18,7 @@ inline cudaError_t prepare_smem(K kernel, size_t smem) {
 // Persistent launch.  wpc == 1: blocks of `cpb` one-warp chains; wpc > 1:
 // blocks of one chain of wpc warps.  As many blocks as chains need, capped
 // at what stays resident; each block then walks its chain slots.
-template <int W32, int Q, bool SUM>
+template <int W32, int Q, bool SUM, bool REC>
 int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   if (a.wpc > 1) cpb = 1;
@@ -26,7 +26,7 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   if (threads > 128) return (int)cudaErrorInvalidConfiguration;
   const size_t smem =
       (size_t)cpb * slot_words(a.ds.n_nodes, RS, a.wpc) * sizeof(uint32_t);
-  auto kern = mcmc_kernel<W32, Q, SUM>;
+  auto kern = mcmc_kernel<W32, Q, SUM, REC>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
@@ -60,10 +60,15 @@ int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
+// Recording launches (recorded moves or a trace) go to the _rec units.
 int launch_mcmc_lo(const RunArgs &a, int w32, int q, bool sum, int cpb,
                    int n_sms, cudaStream_t s);
 int launch_mcmc_hi(const RunArgs &a, int w32, int q, bool sum, int cpb,
                    int n_sms, cudaStream_t s);
+int launch_mcmc_lo_rec(const RunArgs &a, int w32, int q, bool sum, int cpb,
+                       int n_sms, cudaStream_t s);
+int launch_mcmc_hi_rec(const RunArgs &a, int w32, int q, bool sum, int cpb,
+                       int n_sms, cudaStream_t s);
 int launch_batch_lo(const BatchArgs &b, int w32, int q, bool sum, int wpb,
                     int n_sms, cudaStream_t s);
 int launch_batch_hi(const BatchArgs &b, int w32, int q, bool sum, int wpb,
