@@ -701,29 +701,38 @@ int bbs_init_chains(bbs_ctx *c, uint32_t n_chains, const uint32_t *parents) {
     if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
     if (n_chains < 1) return fail(BBS_ERR_INPUT, "need at least one chain");
     const uint32_t n = c->n_nodes;
-    std::vector<uint32_t> pv((size_t)n_chains * n);
+    const size_t tw = (size_t)n * c->W64;
+    std::vector<uint64_t> dm;
     if (parents) {
       for (uint32_t t = 0; t < n_chains; t++) {
         const int r = check_parent_vector(parents + (size_t)t * n, n);
         if (r != BBS_OK) return r;
       }
-      std::memcpy(pv.data(), parents, sizeof(uint32_t) * pv.size());
-    } else {
-      random_parents(c->params.seed, c->n_genes, n_chains, pv.data());
+      dm.resize(tw * n_chains);
+      for (uint32_t t = 0; t < n_chains; t++)
+        parent_to_matrix(parents + (size_t)t * n, n, nullptr, dm.data() + t * tw);
     }
-    const size_t tw = (size_t)n * c->W64;
-    std::vector<uint64_t> dm(tw * n_chains);
-    for (uint32_t t = 0; t < n_chains; t++)
-      parent_to_matrix(pv.data() + (size_t)t * n, n, nullptr, dm.data() + t * tw);
     free_chains(c);
-    cudaError_t e = cudaMalloc(&c->d_rows, sizeof(uint64_t) * dm.size());
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_best, sizeof(uint64_t) * dm.size());
+    const size_t words = tw * n_chains;
+    cudaError_t e = cudaMalloc(&c->d_rows, sizeof(uint64_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_best, sizeof(uint64_t) * words);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_states, sizeof(ChainState) * n_chains);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(c->d_rows, dm.data(), sizeof(uint64_t) * dm.size(),
+    if (e == cudaSuccess && parents)
+      e = cudaMemcpyAsync(c->d_rows, dm.data(), sizeof(uint64_t) * words,
                           cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && !parents) {
+      // random initial trees drawn on the device (the host helper
+      // bbs_random_parent_vectors gives the same trees)
+      TreeArgs ta{};
+      ta.ds = c->d_ds;
+      ta.md = c->d_md;
+      ta.n_chains = (int)n_chains;
+      ta.rows = reinterpret_cast<uint32_t *>(c->d_rows);
+      ta.max_nodes = (int)n;
+      e = (cudaError_t)launch_trees(ta, c->stream);
+    }
     if (e == cudaSuccess)
-      e = cudaMemsetAsync(c->d_best, 0, sizeof(uint64_t) * dm.size(), c->stream);
+      e = cudaMemsetAsync(c->d_best, 0, sizeof(uint64_t) * words, c->stream);
     if (e != cudaSuccess) {
       free_chains(c);
       return cuda_fail((int)e, "bbs_init_chains");
@@ -1601,33 +1610,37 @@ int bbs_batch_init_chains(bbs_batch *b, uint32_t cpd) {
         words = (words + 7) & ~(size_t)7;  // 32-byte aligned rows
       }
     b->row_words = words;
-    std::vector<uint32_t> rows(words, 0u);
-    for (uint32_t d = 0; d < b->n_datasets; d++) {
-      const uint32_t n = b->n_genes[d] + 1;
-      std::vector<uint32_t> pv((size_t)cpd * n);
-      random_parents(b->md[d].seed, b->n_genes[d], cpd, pv.data());
-      std::vector<uint64_t> dm((size_t)n * words64(n));
-      for (uint32_t k = 0; k < cpd; k++) {
-        parent_to_matrix(pv.data() + (size_t)k * n, n, nullptr, dm.data());
-        std::memcpy(rows.data() + b->chain_off[d * cpd + k], dm.data(),
-                    sizeof(uint64_t) * dm.size());
-      }
-    }
+    uint32_t max_nodes = 0;
+    for (uint32_t d = 0; d < b->n_datasets; d++)
+      max_nodes = std::max(max_nodes, b->n_genes[d] + 1);
     cudaError_t e = cudaMalloc(&b->d_rows, sizeof(uint32_t) * words);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_best, sizeof(uint32_t) * words);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_states, sizeof(ChainState) * n_chains);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_ds, sizeof(uint32_t) * n_chains);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_off, sizeof(uint64_t) * n_chains);
     if (e == cudaSuccess)
-      e = cudaMemcpy(b->d_rows, rows.data(), sizeof(uint32_t) * words,
-                     cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(b->d_best, 0, sizeof(uint32_t) * words);
+      e = cudaMemsetAsync(b->d_rows, 0, sizeof(uint32_t) * words, b->stream);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(b->d_best, 0, sizeof(uint32_t) * words, b->stream);
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_chain_ds, b->chain_ds.data(), sizeof(uint32_t) * n_chains,
                      cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
       e = cudaMemcpy(b->d_chain_off, b->chain_off.data(), sizeof(uint64_t) * n_chains,
                      cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      // every dataset's random initial trees, drawn on the device
+      TreeArgs ta{};
+      ta.ds = b->d_ds;
+      ta.md = b->d_md;
+      ta.chain_ds = b->d_chain_ds;
+      ta.chain_off = b->d_chain_off;
+      ta.chains_per_dataset = (int)cpd;
+      ta.n_chains = (int)n_chains;
+      ta.rows = b->d_rows;
+      ta.max_nodes = (int)max_nodes;
+      e = (cudaError_t)launch_trees(ta, b->stream);
+    }
     if (e != cudaSuccess) {
       batch_free_chains(b);
       return cuda_fail((int)e, "bbs_batch_init_chains");

@@ -46,6 +46,90 @@ static int launch_init_t(const InitArgs &a, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
+// Random initial trees (TreeArgs): one warp per chain.  The lanes draw
+// the code and count node degrees; lane 0 decodes it in linear time,
+// always taking the smallest leaf (the order of src/MutationTree.hpp:
+// 454-463); the lanes then write each node's ancestor row (the node, its
+// ancestors and the root, as parent_vector_to_matrix does).
+inline constexpr int kTreeWords = 3 * 256;  // shared words per warp
+
+__global__ void __launch_bounds__(128) tree_kernel(const TreeArgs a) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int chain = blockIdx.x * (blockDim.x >> 5) + wib;
+  if (chain >= a.n_chains) return;
+  const uint32_t d = a.chain_ds != nullptr ? a.chain_ds[chain] : 0u;
+  const int n = a.ds[d].n_nodes;
+  const uint64_t seed = a.md[d].seed;
+  const uint32_t local =
+      (uint32_t)chain - d * (uint32_t)a.chains_per_dataset;
+  uint32_t *code = smem + (size_t)wib * kTreeWords;
+  uint32_t *deg = code + 256;
+  uint32_t *par = deg + 256;
+  const int len = n - 2;
+  for (int i = lane; i < n; i += 32) deg[i] = 1u;
+  __syncwarp();
+  const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+  for (int i4 = 4 * lane; i4 < len; i4 += 128) {
+    const uint4 r = philox4x32_10(make_uint4((uint32_t)i4, local, 0x7265u, 0u),
+                                  key);
+    const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (i4 + k < len) {
+        const uint32_t v = __umulhi(rr[k], (uint32_t)n);
+        code[i4 + k] = v;
+        atomicAdd(&deg[v], 1u);
+      }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    // deg counts the remaining edges of every node not yet removed; every
+    // node below ptr with degree 1 has been removed already
+    int ptr = 0;
+    while (ptr < n && deg[ptr] != 1u) ptr++;
+    int leaf = ptr;
+    for (int i = 0; i < len; i++) {
+      const uint32_t v = code[i];
+      par[leaf] = v;
+      if (--deg[v] == 1u && (int)v < ptr) {
+        leaf = (int)v;
+      } else {
+        ptr++;
+        while (ptr < n && deg[ptr] != 1u) ptr++;
+        leaf = ptr;
+      }
+    }
+    par[leaf < n ? leaf : 0] = (uint32_t)(n - 1);
+    par[n - 1] = (uint32_t)(n - 1);
+  }
+  __syncwarp();
+  const int RS = 2 * ((n + 63) / 64), root = n - 1;
+  uint32_t *out = a.chain_off != nullptr ? a.rows + a.chain_off[chain]
+                                         : a.rows + (size_t)chain * n * RS;
+  for (int x = lane; x < n; x += 32)
+    for (int k = 0; k < RS; k++) {
+      uint32_t v = 0;
+      int y = x;
+      for (int step = 0; step <= n; step++) {
+        if ((y >> 5) == k) v |= 1u << (y & 31);
+        if (y == root) break;
+        y = (int)par[y];
+      }
+      out[(size_t)x * RS + k] = v;
+    }
+}
+
+int launch_trees(const TreeArgs &a, void *stream) {
+  constexpr int WPB = 4;
+  const size_t smem = (size_t)WPB * kTreeWords * sizeof(uint32_t);
+  cudaError_t e = prepare_smem(tree_kernel, smem);
+  if (e != cudaSuccess) return (int)e;
+  tree_kernel<<<(a.n_chains + WPB - 1) / WPB, WPB * 32, smem,
+                (cudaStream_t)stream>>>(a);
+  return (int)cudaGetLastError();
+}
+
 int launch_init(const InitArgs &a, int w32, bool sum, void *stream) {
   cudaStream_t s = (cudaStream_t)stream;
   switch (w32 * 2 + (sum ? 1 : 0)) {

@@ -112,6 +112,21 @@ struct InitArgs {
   int max_nodes;             // shared memory is sized for this
 };
 
+// Random initial trees on the device: per chain a uniform Pruefer code
+// from Philox (seed of the chain's dataset, stream 0x7265, counter (entry
+// group, chain number in its dataset)), decoded smallest leaf first, as
+// ancestor rows.  Same trees as the host's bbs_random_parent_vectors.
+struct TreeArgs {
+  const DatasetDev *ds;      // [n_datasets]
+  const ModelDev *md;
+  const uint32_t *chain_ds;  // null: every chain uses dataset 0
+  const uint64_t *chain_off; // null: chain * n_nodes * RS
+  int chains_per_dataset;    // chain number in its dataset: c - d * this
+  int n_chains;
+  uint32_t *rows;
+  int max_nodes;             // shared memory is sized for this
+};
+
 struct ScoreArgs {
   DatasetDev ds;
   const uint32_t *rows;  // [n_trees][n_nodes][RS]
@@ -152,6 +167,7 @@ int launch_batch(const BatchArgs &b, int w32, int q, bool sum,
 // Launch groups: every chain of a launch must store its rows with the
 // stride rs_of_w32(w32) of the launch (w32 at least the chains' own).
 int launch_init(const InitArgs &a, int w32, bool sum, void *stream);
+int launch_trees(const TreeArgs &a, void *stream);
 int launch_score(const ScoreArgs &a, int q, void *stream);
 int launch_apply(const ApplyArgs &a, void *stream);
 int launch_grad(const GradArgs &a, int q, void *stream);

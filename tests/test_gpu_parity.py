@@ -393,3 +393,20 @@ def test_autotune_keeps_chain_state(native):
         q, wpc, cpb = c.launch()
         assert 1 <= q <= 4 and 1 <= wpc <= 4 and 1 <= cpb <= 4
         c.run(50)  # continues from the saved state
+
+
+@pytest.mark.parametrize("G", [2, 3, 31, 32, 63, 64, 95, 127, 128, 200, 255])
+def test_device_initial_trees_match_host(native, orc, G):
+    """Random initial trees drawn on the device are the host helper's
+    trees for the same seed (bbs_random_parent_vectors)."""
+    m, _, _ = D.generate_dataset(G, G, 20, 1e-3, 0.2, 0.1, 0.0)
+    mut, known = D.matrix_to_bits(m)
+    seed = 0x5EED0000 + G
+    p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=seed)
+    with native.Context(mut, known, 20, G, p) as c:
+        c.init_chains(37)
+        dm = c.chains()["dm"]
+    host = native.random_parents(seed, G, 37)
+    for t in range(37):
+        _, want = orc.parent_to_matrix(host[t])
+        assert (dm[t] == want).all(), t
