@@ -223,7 +223,10 @@ struct bbs_ctx {
   ModelDev *d_md = nullptr;
   float *d_terms = nullptr;
   uint32_t n_chains = 0;
-  uint32_t *d_rows = nullptr, *d_best = nullptr;
+  uint32_t *d_rows = nullptr, *d_best = nullptr;  // d_best: K slots per chain
+  uint32_t K = 1;                  // co-optimal trees kept per chain
+  uint64_t *d_lhash = nullptr;     // [n_chains][K] when K > 1
+  float *d_lbeta = nullptr;
   ChainState *d_states = nullptr;
   int *d_status = nullptr;
   int *h_cancel = nullptr;        // mapped pinned flag
@@ -240,8 +243,12 @@ void free_chains(bbs_ctx *c) {
   cudaFree(c->d_rows);
   cudaFree(c->d_best);
   cudaFree(c->d_states);
+  cudaFree(c->d_lhash);
+  cudaFree(c->d_lbeta);
   c->d_rows = c->d_best = nullptr;
   c->d_states = nullptr;
+  c->d_lhash = nullptr;
+  c->d_lbeta = nullptr;
   c->n_chains = 0;
 }
 
@@ -278,6 +285,9 @@ int check_params(const bbs_params *p) {
     return fail(BBS_ERR_INPUT, "unknown error move %u", p->error_move);
   if (p->error_move != BBS_ERROR_BETA_WALK && !(p->error_step > 0.0f))
     return fail(BBS_ERR_INPUT, "error_step must be positive");
+  if (p->treelist_size > BBS_MAX_TREELIST_PER_CHAIN)
+    return fail(BBS_ERR_INPUT, "treelist_size %u above %d", p->treelist_size,
+                BBS_MAX_TREELIST_PER_CHAIN);
   return BBS_OK;
 }
 
@@ -341,6 +351,7 @@ void prepare_dataset(const bbs_params *params, uint32_t n_cells,
   md.score_mode = (int32_t)params->score_mode;
   md.error_move = (int32_t)params->error_move;
   md.error_step = params->error_step;
+  md.treelist = (int32_t)std::max(1u, params->treelist_size);
   md.seed = params->seed;
   h.terms[0] = alpha;
   h.terms[1] = bm;
@@ -387,6 +398,7 @@ void bbs_params_default(bbs_params *p) {
   p->score_mode = BBS_SCORE_MAX;
   p->error_move = BBS_ERROR_BETA_WALK;
   p->error_step = 1.2f;
+  p->treelist_size = 1;
 }
 
 int bbs_pruefer_to_parent_vector(const uint32_t *code, uint32_t code_len,
@@ -714,9 +726,14 @@ int bbs_init_chains(bbs_ctx *c, uint32_t n_chains, const uint32_t *parents) {
     }
     free_chains(c);
     const size_t words = tw * n_chains;
+    c->K = (uint32_t)c->md.treelist;
     cudaError_t e = cudaMalloc(&c->d_rows, sizeof(uint64_t) * words);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_best, sizeof(uint64_t) * words);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_best, sizeof(uint64_t) * words * c->K);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_states, sizeof(ChainState) * n_chains);
+    if (e == cudaSuccess && c->K > 1)
+      e = cudaMalloc(&c->d_lhash, sizeof(uint64_t) * n_chains * c->K);
+    if (e == cudaSuccess && c->K > 1)
+      e = cudaMalloc(&c->d_lbeta, sizeof(float) * n_chains * c->K);
     if (e == cudaSuccess && parents)
       e = cudaMemcpyAsync(c->d_rows, dm.data(), sizeof(uint64_t) * words,
                           cudaMemcpyHostToDevice, c->stream);
@@ -732,7 +749,8 @@ int bbs_init_chains(bbs_ctx *c, uint32_t n_chains, const uint32_t *parents) {
       e = (cudaError_t)launch_trees(ta, c->stream);
     }
     if (e == cudaSuccess)
-      e = cudaMemsetAsync(c->d_best, 0, sizeof(uint64_t) * words, c->stream);
+      e = cudaMemsetAsync(c->d_best, 0, sizeof(uint64_t) * words * c->K,
+                          c->stream);
     if (e != cudaSuccess) {
       free_chains(c);
       return cuda_fail((int)e, "bbs_init_chains");
@@ -771,6 +789,8 @@ int start_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *d_moves,
   a.n_steps = (int)n_steps;
   a.rows = c->d_rows;
   a.best_rows = c->d_best;
+  a.list_hash = c->K > 1 ? c->d_lhash : nullptr;
+  a.list_beta = c->K > 1 ? c->d_lbeta : nullptr;
   a.states = c->d_states;
   a.moves = d_moves;
   a.trace = d_trace;
@@ -899,16 +919,26 @@ int bbs_autotune(bbs_ctx *c, uint32_t probe_steps, float *best_ms) {
     if (probe_steps == 0) probe_steps = 64;
     // Keep the chains as they are: save, probe, restore.
     const size_t rows_bytes = sizeof(uint64_t) * c->n_chains * c->n_nodes * c->W64;
-    DevBuf<uint8_t> save_rows, save_best, save_states;
+    const size_t best_bytes = rows_bytes * c->K;
+    const size_t list_bytes = c->K > 1 ? (size_t)c->n_chains * c->K : 0;
+    DevBuf<uint8_t> save_rows, save_best, save_states, save_lh, save_lb;
     BBS_CUDA(save_rows.alloc(rows_bytes), "cudaMalloc");
-    BBS_CUDA(save_best.alloc(rows_bytes), "cudaMalloc");
+    BBS_CUDA(save_best.alloc(best_bytes), "cudaMalloc");
     BBS_CUDA(save_states.alloc(sizeof(ChainState) * c->n_chains), "cudaMalloc");
+    if (list_bytes) {
+      BBS_CUDA(save_lh.alloc(list_bytes * sizeof(uint64_t)), "cudaMalloc");
+      BBS_CUDA(save_lb.alloc(list_bytes * sizeof(float)), "cudaMalloc");
+    }
     auto copy = [&](void *dst, const void *src, size_t b) {
       return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, c->stream);
     };
     BBS_CUDA(copy(save_rows.p, c->d_rows, rows_bytes), "save");
-    BBS_CUDA(copy(save_best.p, c->d_best, rows_bytes), "save");
+    BBS_CUDA(copy(save_best.p, c->d_best, best_bytes), "save");
     BBS_CUDA(copy(save_states.p, c->d_states, sizeof(ChainState) * c->n_chains), "save");
+    if (list_bytes) {
+      BBS_CUDA(copy(save_lh.p, c->d_lhash, list_bytes * sizeof(uint64_t)), "save");
+      BBS_CUDA(copy(save_lb.p, c->d_lbeta, list_bytes * sizeof(float)), "save");
+    }
     const int groups = (int)((c->n_cells + 31) / 32);
     const int qmax = w32_of_nodes((int)c->n_nodes) > 4 ? 2 : kMaxQ;
     const int q0 = c->q, w0 = c->wpc, b0 = c->cpb;
@@ -933,9 +963,15 @@ int bbs_autotune(bbs_ctx *c, uint32_t probe_steps, float *best_ms) {
             bb = cpb;
           }
           BBS_CUDA(copy(c->d_rows, save_rows.p, rows_bytes), "restore");
-          BBS_CUDA(copy(c->d_best, save_best.p, rows_bytes), "restore");
+          BBS_CUDA(copy(c->d_best, save_best.p, best_bytes), "restore");
           BBS_CUDA(copy(c->d_states, save_states.p,
                         sizeof(ChainState) * c->n_chains), "restore");
+          if (list_bytes) {
+            BBS_CUDA(copy(c->d_lhash, save_lh.p, list_bytes * sizeof(uint64_t)),
+                     "restore");
+            BBS_CUDA(copy(c->d_lbeta, save_lb.p, list_bytes * sizeof(float)),
+                     "restore");
+          }
         }
       }
     c->q = bq;
@@ -977,7 +1013,7 @@ int bbs_get_best(bbs_ctx *c, uint64_t *am, uint64_t *dm, uint32_t *parent,
     const uint32_t n = c->n_nodes;
     const size_t tw = (size_t)n * c->W64;
     std::vector<uint64_t> rows(tw);
-    BBS_CUDA(cudaMemcpy(rows.data(), c->d_best + (size_t)best * tw * 2,
+    BBS_CUDA(cudaMemcpy(rows.data(), c->d_best + (size_t)best * c->K * tw * 2,
                         sizeof(uint64_t) * tw, cudaMemcpyDeviceToHost), "best copy");
     if (dm) std::memcpy(dm, rows.data(), sizeof(uint64_t) * tw);
     if (am) bbs_dm_to_am(rows.data(), n, am);
@@ -1030,6 +1066,61 @@ int bbs_get_chains(bbs_ctx *c, uint64_t *dm, float *alpha, float *beta,
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_get_chains");
+  }
+}
+
+int bbs_get_treelist(bbs_ctx *c, uint32_t max_trees, uint64_t *dm,
+                     float *betas, float *score, uint32_t *n_trees) {
+  try {
+    if (!c || !dm || !n_trees) return fail(BBS_ERR_INPUT, "NULL argument");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (c->n_chains == 0) return fail(BBS_ERR_STATE, "no chains");
+    *n_trees = 0;
+    std::vector<ChainState> st(c->n_chains);
+    BBS_CUDA(cudaMemcpy(st.data(), c->d_states, sizeof(ChainState) * st.size(),
+                        cudaMemcpyDeviceToHost), "state copy");
+    int best = -1;
+    for (uint32_t i = 0; i < c->n_chains; i++) {
+      if (!st[i].has_best) continue;
+      if (best < 0 || st[i].best_score > st[best].best_score) best = (int)i;
+    }
+    if (best < 0) return fail(BBS_ERR_STATE, "no steps have been run");
+    const float top = st[best].best_score;
+    if (score) *score = top;
+    const size_t tw = (size_t)c->n_nodes * c->W64;
+    std::vector<uint64_t> rows(tw * c->K);
+    std::vector<float> lb(c->K);
+    uint32_t found = 0;
+    // the bbs_get_best chain first, then the others in index order
+    for (uint32_t k = 0; k <= c->n_chains && found < max_trees; k++) {
+      const uint32_t i = k == 0 ? (uint32_t)best : k - 1;
+      if (k > 0 && i == (uint32_t)best) continue;
+      if (!st[i].has_best || st[i].best_score != top) continue;
+      const uint32_t cnt = c->K > 1 ? std::min(st[i].list_count, c->K) : 1u;
+      BBS_CUDA(cudaMemcpy(rows.data(), c->d_best + (size_t)i * c->K * tw * 2,
+                          sizeof(uint64_t) * tw * cnt, cudaMemcpyDeviceToHost),
+               "tree list copy");
+      if (c->K > 1)
+        BBS_CUDA(cudaMemcpy(lb.data(), c->d_lbeta + (size_t)i * c->K,
+                            sizeof(float) * cnt, cudaMemcpyDeviceToHost),
+                 "tree list copy");
+      else
+        lb[0] = st[i].best_beta;
+      for (uint32_t j = 0; j < cnt && found < max_trees; j++) {
+        const uint64_t *t = rows.data() + j * tw;
+        bool dup = false;
+        for (uint32_t u = 0; u < found && !dup; u++)
+          dup = std::memcmp(dm + u * tw, t, sizeof(uint64_t) * tw) == 0;
+        if (dup) continue;
+        std::memcpy(dm + found * tw, t, sizeof(uint64_t) * tw);
+        if (betas) betas[found] = lb[j];
+        found++;
+      }
+    }
+    *n_trees = found;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_get_treelist");
   }
 }
 

@@ -418,6 +418,36 @@ __device__ __forceinline__ float pair_score(int d, int m, float pdb,
   return s;
 }
 
+// 64-bit hash of a tree's ancestor rows, the same in every lane: a mix of
+// each word with its position, summed and xor-ed over the warp.
+template <int W32>
+__device__ __forceinline__ uint64_t tree_hash(const uint32_t *rows, int n,
+                                              int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  uint32_t h0 = 0, h1 = 0;
+#pragma unroll
+  for (int r = 0; r < W32; r++) {
+    const int x = 32 * r + lane;
+    if (x < n) {
+      uint32_t a[W32];
+      ld_row<W32>(rows + x * RS, a);
+#pragma unroll
+      for (int k = 0; k < W32; k++) {
+        uint32_t v = a[k] ^ (0x9E3779B9u * (uint32_t)(x * W32 + k + 1));
+        v *= 0x85EBCA6Bu;
+        v ^= v >> 13;
+        v *= 0xC2B2AE35u;
+        v ^= v >> 16;
+        h0 += v;
+        h1 ^= v * 0x27D4EB2Fu + (uint32_t)x;
+      }
+    }
+  }
+  h0 = __reduce_add_sync(BBS_FULL_MASK, h0);
+  h1 = __reduce_xor_sync(BBS_FULL_MASK, h1);
+  return ((uint64_t)h1 << 32) | h0;
+}
+
 // Per lane: Q cells as observed-0 rows D = K & ~M and observed-1 rows M.
 template <int W32, int Q>
 struct Cells {

@@ -44,6 +44,7 @@ struct ModelDev {
   int32_t error_move;  // 0: reference beta walk, 1: preconditioned random
                        // walk on (logit alpha, logit beta), 2: Langevin
   float error_step;    // step size of error moves 1 and 2
+  int32_t treelist;    // co-optimal trees kept per chain (1: the best only)
   uint64_t seed;       // Philox key
 };
 
@@ -60,7 +61,8 @@ struct ChainState {
   int32_t best_sk, best_sm;
   uint64_t steps_done;              // Philox step counter
   uint32_t err_proposed, err_accepted;
-  uint32_t pad[8];
+  uint32_t list_count;              // trees in the chain's co-optimal list
+  uint32_t pad[7];
 };
 static_assert(sizeof(ChainState) == 128, "ChainState layout");
 
@@ -69,7 +71,10 @@ struct RunArgs {
   ModelDev md;
   int n_chains, n_steps;
   uint32_t *rows;       // [n_chains][n_nodes][RS] current trees
-  uint32_t *best_rows;  // [n_chains][n_nodes][RS] best proposals
+  uint32_t *best_rows;  // [n_chains][treelist][n_nodes][RS] best proposal
+                        // and the trees tied with it
+  uint64_t *list_hash;  // [n_chains][treelist] tree hashes (treelist > 1)
+  float *list_beta;     // [n_chains][treelist]
   ChainState *states;
   const bbs_raw_move *moves;  // [n_chains][n_steps] or null
   bbs_step_trace *trace;      // [n_chains][n_steps] or null

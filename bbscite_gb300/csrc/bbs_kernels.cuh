@@ -110,7 +110,8 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
 template <int W32, int Q, bool SUM>
 __device__ __forceinline__ void run_chain(
     const DatasetDev &ds, const ModelDev &md, uint32_t chain_id,
-    uint32_t *g, uint32_t *gbest, ChainState *gstate,
+    uint32_t *g, uint32_t *gbest, uint64_t *lhash, float *lbeta, int K,
+    ChainState *gstate,
     const bbs_raw_move *moves, bbs_step_trace *trace, int n_steps,
     const volatile int *cancel, int *status, uint32_t *buf0, uint32_t *buf1,
     int *part, volatile int *sflag, Cells<W32, Q> &cb, bool resident, int wpc,
@@ -130,6 +131,7 @@ __device__ __forceinline__ void run_chain(
         best_beta = st.best_beta;
   int bsk = st.best_sk, bsm = st.best_sm;
   uint32_t err_prop = st.err_proposed, err_acc = st.err_accepted;
+  uint32_t lcount = st.list_count;  // co-optimal trees listed (K > 1)
   const bool learn = md.error_move != 0;
   int i = 0;
   bool cancelled = false;
@@ -230,6 +232,29 @@ __device__ __forceinline__ void run_chain(
       bsk = sk;
       bsm = sm;
       copy_rows_part<W32>(scored, gbest, n, wpc, wic, lane);
+      if (K > 1) {
+        // a new best: the co-optimal list restarts with it
+        const uint64_t h = tree_hash<W32>(scored, n, lane);
+        if (wic == 0 && lane == 0) {
+          lhash[0] = h;
+          lbeta[0] = pbeta;
+        }
+        lcount = 1;
+      }
+    } else if (K > 1 && psmax == best_score && lcount < (uint32_t)K) {
+      // a tie with the best: listed when it is a tree not listed yet
+      const uint64_t h = tree_hash<W32>(scored, n, lane);
+      const bool seen =
+          __any_sync(BBS_FULL_MASK, lane < (int)lcount && lhash[lane] == h);
+      if (!seen) {
+        copy_rows_part<W32>(scored, gbest + (size_t)lcount * n * rs_of_w32(W32),
+                            n, wpc, wic, lane);
+        if (wic == 0 && lane == 0) {
+          lhash[lcount] = h;
+          lbeta[lcount] = pbeta;
+        }
+        lcount++;
+      }
     }
     if (trace != nullptr && wic == 0 && lane == 0) {
       bbs_step_trace *t = trace + i;
@@ -289,6 +314,7 @@ __device__ __forceinline__ void run_chain(
     o.steps_done = st.steps_done + (uint64_t)i;
     o.err_proposed = err_prop;
     o.err_accepted = err_acc;
+    o.list_count = lcount;
     *gstate = o;
     if (cancelled && status != nullptr) atomicOr(status, 1);
   }
@@ -333,9 +359,13 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
       if (a.moves != nullptr) moves = a.moves + (size_t)chain * a.n_steps;
       if (a.trace != nullptr) trace = a.trace + (size_t)chain * a.n_steps;
     }
+    const int K = a.list_hash != nullptr ? a.md.treelist : 1;
     run_chain<W32, Q, SUM>(
         a.ds, a.md, (uint32_t)chain, a.rows + (size_t)chain * n * RS,
-        a.best_rows + (size_t)chain * n * RS, a.states + chain, moves, trace,
+        a.best_rows + (size_t)chain * K * n * RS,
+        K > 1 ? a.list_hash + (size_t)chain * K : nullptr,
+        K > 1 ? a.list_beta + (size_t)chain * K : nullptr, K, a.states + chain,
+        moves, trace,
         a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, cb, resident,
         wpc, wic, lane);
   }
@@ -373,7 +403,7 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
     // chains draw the same moves here as in a one-dataset run.
     const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
     run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
-                           b.states + chain, nullptr, nullptr, b.n_steps,
+                           nullptr, nullptr, 1, b.states + chain, nullptr, nullptr, b.n_steps,
                            b.cancel, b.status, buf0, buf1d, part, sflag, cb,
                            resident, 1, 0, lane);
     (void)buf1;
@@ -434,7 +464,8 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
     o.steps_done = 0;
     o.err_proposed = 0;
     o.err_accepted = 0;
-    for (int k = 0; k < 8; k++) o.pad[k] = 0;
+    o.list_count = 0;
+    for (int k = 0; k < 7; k++) o.pad[k] = 0;
     a.states[chain] = o;
   }
 }

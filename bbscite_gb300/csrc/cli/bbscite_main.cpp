@@ -4,11 +4,14 @@
 // of the reference:
 //   <base>_ml0.gv, <base>_ml0.newick, <base>_ml0_beta.txt,
 //   <base>_ml0_am.txt, <base>_ml0_dm.txt
-// with <base> from -o or the input path without its suffix.  The size
+// with <base> from -o or the input path without its suffix.  Trees tied
+// with the best (SCITE's tree list, -max_treelist_size, which the
+// reference parses but does not use) follow as _ml1, _ml2, ...  The size
 // limits are BBS_MAX_CELLS cells and BBS_MAX_GENES genes instead of the
 // FPGA builds' 64/96.  "Move generation makespan" reports the host setup
 // time (context and initial trees): the moves are drawn inside the chain
 // kernel.
+#include <algorithm>
 #include <fstream>
 #include <iostream>
 #include <sstream>
@@ -149,25 +152,33 @@ int main(int argc, char **argv) {
     const float runtime = app.run_simulation();
     std::cout << "Time elapsed: " << runtime << " ms" << std::endl;
 
-    AncestorMatrix best_am = app.get_best_am();
-    AncestorMatrix best_dm = app.get_best_dm();
-    const float best_beta = app.get_best_beta();
-    MutationTree tree(best_am, best_dm, n_genes, best_beta);
+    // <base>_ml<i> for every co-optimal tree (SCITE's tree list; the
+    // reference writes only _ml0, which is the best tree here too)
     const std::string base = parameters.get_output_path_base();
-    {
-      std::ofstream out(base + "_ml0.gv");
-      out << tree.to_graphviz();
+    auto list = app.get_treelist(
+        std::max<uint32_t>(1u, parameters.get_max_n_best_trees()));
+    for (size_t i = 0; i < list.size(); i++) {
+      AncestorMatrix best_dm = list[i].first;
+      const float best_beta = list[i].second;
+      AncestorMatrix best_am(best_dm.size());
+      check(bbs_dm_to_am(best_dm.data(), n_genes + 1, best_am.data()));
+      MutationTree tree(best_am, best_dm, n_genes, best_beta);
+      const std::string ml = base + "_ml" + std::to_string(i);
+      {
+        std::ofstream out(ml + ".gv");
+        out << tree.to_graphviz();
+      }
+      {
+        std::ofstream out(ml + ".newick");
+        out << tree.to_newick();
+      }
+      {
+        std::ofstream out(ml + "_beta.txt");
+        out << best_beta << std::endl;
+      }
+      write_matrix(ml + "_am.txt", best_am, n_genes + 1);
+      write_matrix(ml + "_dm.txt", best_dm, n_genes + 1);
     }
-    {
-      std::ofstream out(base + "_ml0.newick");
-      out << tree.to_newick();
-    }
-    {
-      std::ofstream out(base + "_ml0_beta.txt");
-      out << best_beta << std::endl;
-    }
-    write_matrix(base + "_ml0_am.txt", best_am, n_genes + 1);
-    write_matrix(base + "_ml0_dm.txt", best_dm, n_genes + 1);
   } catch (Error const &e) {
     std::cerr << "Error: " << e.what() << std::endl;
     return 1;

@@ -53,7 +53,7 @@ class Params(C.Structure):
                 ("prob_swap_nodes", C.c_float),
                 ("prob_swap_subtrees", C.c_float),
                 ("beta_jump_scaling_chi", C.c_float), ("gamma", C.c_float),
-                ("reserved0", C.c_uint32), ("seed", C.c_uint64),
+                ("treelist_size", C.c_uint32), ("seed", C.c_uint64),
                 ("score_mode", C.c_uint32), ("error_move", C.c_uint32),
                 ("error_step", C.c_float), ("reserved1", C.c_uint32)]
 
@@ -99,6 +99,7 @@ def lib():
         "bbs_get_best": (C.c_int, [v, v, v, v, v, v, v, v]),
         "bbs_get_chains": (C.c_int, [v, v, v, v, v, v, v]),
         "bbs_get_best_alpha": (C.c_int, [v, v]),
+        "bbs_get_treelist": (C.c_int, [v, u32, v, v, v, v]),
         "bbs_batch_create": (C.c_int, [v, u32, v, v, v, v, v]),
         "bbs_batch_destroy": (None, [v]),
         "bbs_batch_init_chains": (C.c_int, [v, u32]),
@@ -322,6 +323,16 @@ class Context:
                                    _p(score), _p(counts), _p(err)))
         return dict(dm=dm, alpha=alpha, beta=beta, score=score,
                     counts=counts, err_stats=err)
+
+    def treelist(self, max_trees: int = 128) -> dict:
+        """Distinct trees tied with the best proposal (up to
+        params.treelist_size per chain): dm (k x n x W), betas, score."""
+        dm = np.zeros((max_trees, self.n_nodes, self.W), dtype=np.uint64)
+        betas = np.zeros(max_trees, dtype=np.float32)
+        score, k = C.c_float(), C.c_uint32()
+        check(lib().bbs_get_treelist(self._h, max_trees, _p(dm), _p(betas),
+                                     C.byref(score), C.byref(k)))
+        return dict(dm=dm[:k.value], betas=betas[:k.value], score=score.value)
 
     def best_alpha(self) -> float:
         a = C.c_float()

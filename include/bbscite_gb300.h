@@ -47,6 +47,7 @@ extern "C" {
 
 #define BBS_MAX_GENES 255   /* replaces the compile-time 63/95 caps */
 #define BBS_MAX_CELLS 65535 /* integer class totals stay exact in FP32 */
+#define BBS_MAX_TREELIST_PER_CHAIN 16
 
 /* src/MoveType.hpp:23-42 */
 #define BBS_MOVE_CHANGE_BETA 0
@@ -66,7 +67,8 @@ typedef struct bbs_params {
   float prob_swap_subtrees;
   float beta_jump_scaling_chi; /* -x   */
   float gamma;                 /* -g   */
-  uint32_t reserved0;
+  uint32_t treelist_size;      /* co-optimal trees kept per chain (1: the best
+                                  only), at most BBS_MAX_TREELIST_PER_CHAIN */
   uint64_t seed; /* Philox key for moves and random initial trees */
   /* Extensions without a counterpart in the reference (defaults reproduce
    * it): the score and the error-rate move taken with probability
@@ -223,6 +225,16 @@ BBS_API int bbs_last_run_ms(const bbs_ctx *ctx, float *ms);
 BBS_API int bbs_get_best(bbs_ctx *ctx, uint64_t *am, uint64_t *dm, uint32_t *parent,
                  float *beta, float *score, uint64_t *counts,
                  uint32_t *chain);
+/* The co-optimal tree list: SCITE's -max_treelist_size, parsed but
+ * unused by the reference (src/Parameters.hpp:223-231).  Each chain keeps
+ * up to params.treelist_size distinct trees whose score equals its best
+ * proposal's; this gathers the distinct trees of every chain whose best
+ * equals the overall best, in chain order, the bbs_get_best tree first.
+ * dm: max_trees x n_nodes x W ancestor rows; betas: max_trees (may be
+ * NULL); *score the common score; *n_trees the number written. */
+BBS_API int bbs_get_treelist(bbs_ctx *ctx, uint32_t max_trees, uint64_t *dm,
+                             float *betas, float *score, uint32_t *n_trees);
+
 /* The alpha of the best proposal (equal to alpha_mean unless alpha is
  * learned by the error move). */
 BBS_API int bbs_get_best_alpha(bbs_ctx *ctx, float *alpha);

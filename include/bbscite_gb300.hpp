@@ -17,6 +17,7 @@
 #ifndef BBSCITE_GB300_HPP
 #define BBSCITE_GB300_HPP
 
+#include <algorithm>
 #include <chrono>
 #include <cstdint>
 #include <cstdlib>
@@ -233,6 +234,7 @@ class Parameters {
   uint32_t get_chain_length() const { return chain_length.value(); }
   void set_chain_length(uint32_t v) { chain_length = v; }
   uint32_t get_max_n_best_trees() const { return max_n_best_trees; }
+  void set_max_n_best_trees(uint32_t v) { max_n_best_trees = v; }
   float get_alpha_mean() const { return alpha_mean; }
   void set_alpha_mean(float v) { alpha_mean = v; }
   float get_beta_mean() const { return beta_mean; }
@@ -277,6 +279,8 @@ class Parameters {
     p.beta_jump_scaling_chi = beta_jump_scaling_chi;
     p.gamma = gamma;
     p.seed = seed;
+    p.treelist_size = std::max<uint32_t>(
+        1u, std::min<uint32_t>(max_n_best_trees, BBS_MAX_TREELIST_PER_CHAIN));
     p.score_mode = score_mode;
     p.error_move = error_move;
     if (error_step > 0.0f) p.error_step = error_step;
@@ -566,6 +570,24 @@ class Application {
     float a = 0.0f;
     check(bbs_get_best_alpha(ctx.get(), &a));
     return a;
+  }
+  /* The co-optimal tree list (SCITE's -max_treelist_size): up to
+   * max_trees distinct trees tied with the best, the best first, as
+   * descendant matrices with their betas. */
+  std::vector<std::pair<AncestorMatrix, float>> get_treelist(uint32_t max_trees) {
+    const uint32_t n = n_genes + 1, W = bbs_words(n);
+    std::vector<uint64_t> dm((size_t)max_trees * n * W);
+    std::vector<float> betas(max_trees);
+    float score = 0.0f;
+    uint32_t k = 0;
+    check(bbs_get_treelist(ctx.get(), max_trees, dm.data(), betas.data(),
+                           &score, &k));
+    std::vector<std::pair<AncestorMatrix, float>> out;
+    for (uint32_t i = 0; i < k; i++)
+      out.emplace_back(AncestorMatrix(dm.begin() + (size_t)i * n * W,
+                                      dm.begin() + (size_t)(i + 1) * n * W),
+                       betas[i]);
+    return out;
   }
   bbs_ctx *handle() { return ctx.get(); }
 
