@@ -596,11 +596,22 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
 // A cell whose maximum lies more than 80 below r is summed once more
 // against its maximum.  In base-2 units t_j = (s_j - r) log2(e) is affine
 // in (d, m) = (popc(D & A), popc(M & A)), two FMAs per pair.  Adds to
-// acc[6], in fixed point (2^-20 units, so the result does not depend on
-// how cells are split over lanes and warps): sum_c lse_c, the expected
-// class counts E[n00], E[n01], E[n10], E[n11], and sum_c max_j s_cj (the
-// max score).
-inline constexpr float kFixScale = 1048576.0f;  // 2^20
+// acc[6], in fixed point (2^-16 units for scores, 2^-20 for counts, so the
+// result does not depend on how cells are split over lanes and warps):
+// sum_c lse_c, the expected class counts E[n00], E[n01], E[n10], E[n11],
+// and sum_c max_j s_cj (the max score).
+inline constexpr float kFixScale = 1048576.0f;  // 2^20, class counts
+inline constexpr float kScoreScale = 65536.0f;  // 2^16, scores: a cell's
+  // |log-likelihood| stays below 2^15 for any float alpha, beta (at most
+  // 255 genes of |log p| <= 104), so each cell's term fits in 32 bits
+
+// An int64 fixed-point total as a float (hi * 2^32 + lo, one rounding of
+// each part and of their sum; no double-precision arithmetic).
+__device__ __forceinline__ float ll_to_float(long long x) {
+  const int hi = (int)(x >> 32);
+  const unsigned lo = (unsigned)(x & 0xffffffffll);
+  return fmaf((float)hi, 4294967296.0f, __uint2float_rn(lo));
+}
 inline constexpr float kLog2E = 1.44269504088896341f;
 inline constexpr float kLn2 = 0.693147180559945309f;
 
@@ -704,12 +715,12 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     const float inv = 1.0f / z[q];
     const float Ed = ed[q] * inv, Em = em[q] * inv;
     const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
-    acc[0] += __float2ll_rn((r[q] + logf(z[q])) * kFixScale);
-    acc[1] += __float2ll_rn((pd - Ed) * kFixScale);  // E[n00]
-    acc[2] += __float2ll_rn(Ed * kFixScale);         // E[n01]
-    acc[3] += __float2ll_rn((pm - Em) * kFixScale);  // E[n10]
-    acc[4] += __float2ll_rn(Em * kFixScale);         // E[n11]
-    acc[5] += __float2ll_rn(fmaf(mx[q], kLn2, r[q]) * kFixScale);  // max
+    acc[0] += (long long)__float2int_rn((r[q] + logf(z[q])) * kScoreScale);
+    acc[1] += (long long)__float2int_rn((pd - Ed) * kFixScale);  // E[n00]
+    acc[2] += (long long)__float2int_rn(Ed * kFixScale);         // E[n01]
+    acc[3] += (long long)__float2int_rn((pm - Em) * kFixScale);  // E[n10]
+    acc[4] += (long long)__float2int_rn(Em * kFixScale);         // E[n11]
+    acc[5] += (long long)__float2int_rn(fmaf(mx[q], kLn2, r[q]) * kScoreScale);
   }
 }
 
@@ -775,11 +786,23 @@ __device__ __forceinline__ void beta_terms(const DatasetDev &ds, float beta,
   prior = __fsub_rn(r, ds.lg_b);
 }
 
-// The alpha-dependent entries, as the reference's ctor computes them.
-__device__ __forceinline__ void alpha_terms(float alpha, float &l00,
-                                            float &l10) {
-  l00 = (float)log(1.0 - (double)alpha);
+// The same entries in single precision for the learned error moves (no
+// reference counterpart to match, so no double-precision logs): the log
+// table of a proposed (alpha, beta) and logscore_beta.
+__device__ __forceinline__ void alpha_terms_f(float alpha, float &l00,
+                                              float &l10) {
+  l00 = log1pf(-alpha);
   l10 = logf(alpha);
+}
+__device__ __forceinline__ void beta_terms_f(const DatasetDev &ds, float beta,
+                                             float &l01, float &l11,
+                                             float &prior) {
+  l01 = logf(beta);
+  l11 = log1pf(-beta);
+  float r = __fadd_rn(ds.lg_ab, __fmul_rn(__fsub_rn(ds.bpa, 1.0f), l01));
+  r = __fadd_rn(r, __fmul_rn(__fsub_rn(ds.bpb, 1.0f), logf(__fsub_rn(1.0f, beta))));
+  r = __fsub_rn(r, ds.lg_a);
+  prior = __fsub_rn(r, ds.lg_b);
 }
 
 // ------------------------------------------------------------------------

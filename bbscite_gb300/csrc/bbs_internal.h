@@ -52,9 +52,10 @@ struct ModelDev {
 struct ChainState {
   float alpha, beta, score, prior;  // score = data term + log prior(beta)
   float l00, l10, l01, l11;         // log table of (alpha, beta)
-  float grad_a, grad_b;             // gradient of the error-move target in
-                                    // (logit alpha, logit beta)
-  float prec_a, prec_b;             // diagonal preconditioner there
+  float ec[4];                      // class counts n00, n01, n10, n11 of
+                                    // the current tree at the current rates
+                                    // (expected counts for the sum score):
+                                    // the error moves' gradient source
   int32_t sk, sm;                   // class sums (max score)
   uint32_t has_best;
   float best_alpha, best_beta, best_score;

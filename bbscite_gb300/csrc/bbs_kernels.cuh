@@ -98,9 +98,9 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
     }
     sk = sm = 0;
 #pragma unroll
-    for (int i = 0; i < 4; i++) e[i] = (float)((double)acc[i + 1] / kFixScale);
-    smax = __fadd_rn((float)((double)acc[5] / kFixScale), prior);
-    return __fadd_rn((float)((double)acc[0] / kFixScale), prior);
+    for (int i = 0; i < 4; i++) e[i] = ll_to_float(acc[i + 1]) * (1.0f / kFixScale);
+    smax = __fadd_rn(ll_to_float(acc[5]) * (1.0f / kScoreScale), prior);
+    return __fadd_rn(ll_to_float(acc[0]) * (1.0f / kScoreScale), prior);
   }
 }
 
@@ -124,7 +124,7 @@ __device__ __forceinline__ void run_chain(
   uint32_t *cur = buf0, *prop = buf1;
   float alpha = st.alpha, beta = st.beta, score = st.score, prior = st.prior;
   LogTable L{st.l00, st.l10, st.l01, st.l11};
-  ErrorGeom geo{st.grad_a, st.grad_b, st.prec_a, st.prec_b};
+  float ec[4] = {st.ec[0], st.ec[1], st.ec[2], st.ec[3]};
   int csk = st.sk, csm = st.sm;
   bool has_best = st.has_best != 0;
   float best_score = st.best_score, best_alpha = st.best_alpha,
@@ -158,6 +158,7 @@ __device__ __forceinline__ void run_chain(
     const uint32_t *scored = cur;
     float corr = 1.0f;
     float fa = 0.0f, fb = 0.0f, ta = 0.0f, tb = 0.0f;
+    ErrorGeom geo{};  // of the current state, on learned error moves
     uint32_t Dv[W32], Dw[W32];
     if (!err_move) {
       const Realized R = realize_move<W32>(cur, n, beta, raw, lane, Dv, Dw);
@@ -176,7 +177,9 @@ __device__ __forceinline__ void run_chain(
       pbeta = nb;
       beta_terms(ds, pbeta, PL.l01, PL.l11, pprior);
     } else {
-      // (preconditioned) random walk or Langevin step in logit space
+      // (preconditioned) random walk or Langevin step in logit space, with
+      // the geometry of the current state from its class counts
+      geo = error_geometry(ds, alpha, beta, md.gamma, ec);
       float z0, z1;
       error_normals(raw, z0, z1);
       const float eps = md.error_step;
@@ -189,8 +192,8 @@ __device__ __forceinline__ void run_chain(
       pbeta = fminf(fmaxf(sigmoid(tb), 1.0e-7f), 1.0f - 1.0e-7f);
       ta = logit(palpha);
       tb = logit(pbeta);
-      alpha_terms(palpha, PL.l00, PL.l10);
-      beta_terms(ds, pbeta, PL.l01, PL.l11, pprior);
+      alpha_terms_f(palpha, PL.l00, PL.l10);
+      beta_terms_f(ds, pbeta, PL.l01, PL.l11, pprior);
     }
     if (multi) __syncthreads(); else __syncwarp();
     float e[4], psmax;
@@ -198,10 +201,9 @@ __device__ __forceinline__ void run_chain(
     const float pscore = evaluate<W32, Q, SUM>(scored, n, ds, cb, resident, PL,
                                                pprior, wpc, wic, lane, part,
                                                i & 1, e, sk, sm, psmax);
-    ErrorGeom pgeo = geo;
-    if (learn) pgeo = error_geometry(ds, palpha, pbeta, md.gamma, e);
     bool accept;
     if (err_move && learn) {
+      const ErrorGeom pgeo = error_geometry(ds, palpha, pbeta, md.gamma, e);
       const float logj = logf(alpha * (1.0f - alpha)) + logf(beta * (1.0f - beta));
       const float plogj =
           logf(palpha * (1.0f - palpha)) + logf(pbeta * (1.0f - pbeta));
@@ -282,7 +284,8 @@ __device__ __forceinline__ void run_chain(
       score = pscore;
       prior = pprior;
       L = PL;
-      geo = pgeo;
+#pragma unroll
+      for (int k = 0; k < 4; k++) ec[k] = e[k];
       csk = sk;
       csm = sm;
     }
@@ -299,10 +302,8 @@ __device__ __forceinline__ void run_chain(
     o.l10 = L.l10;
     o.l01 = L.l01;
     o.l11 = L.l11;
-    o.grad_a = geo.grad_a;
-    o.grad_b = geo.grad_b;
-    o.prec_a = geo.prec_a;
-    o.prec_b = geo.prec_b;
+#pragma unroll
+    for (int k = 0; k < 4; k++) o.ec[k] = ec[k];
     o.sk = csk;
     o.sm = csm;
     o.has_best = has_best ? 1u : 0u;
@@ -439,7 +440,6 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
   const float S = evaluate<W32, Q, SUM>(rows, n, ds, cb, false, L, prior, 1, 0,
                                         lane, nullptr, 0, e, sk, sm, smax);
   if (lane == 0) {
-    const ErrorGeom geo = error_geometry(ds, alpha, beta, md.gamma, e);
     ChainState o;
     o.alpha = alpha;
     o.beta = beta;
@@ -449,10 +449,8 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
     o.l10 = L.l10;
     o.l01 = L.l01;
     o.l11 = L.l11;
-    o.grad_a = geo.grad_a;
-    o.grad_b = geo.grad_b;
-    o.prec_a = geo.prec_a;
-    o.prec_b = geo.prec_b;
+#pragma unroll
+    for (int k = 0; k < 4; k++) o.ec[k] = e[k];
     o.sk = sk;
     o.sm = sm;
     o.has_best = 0;
