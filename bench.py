@@ -430,7 +430,7 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     At every checkpoint (1,000-step chunks to 20,000 steps, then
     10,000-step chunks) each arm's best tree is scored with the reference's
     max score at the generator's rates (a scale common to both arms: the
-    chains judge proposals at their own sampled rates), and the median over
+    chains rank proposals at their own sampled rates), and the median over
     chains of logit(alpha) and logit(beta) is read.  Per seed: the first
     step count at which the Langevin arm's best is within 0.1 nats of the
     random-walk arm's final best, and for each arm the step count after

@@ -68,7 +68,9 @@ typedef struct bbs_params {
   float beta_jump_scaling_chi; /* -x   */
   float gamma;                 /* -g   */
   uint32_t treelist_size;      /* co-optimal trees kept per chain (1: the best
-                                  only), at most BBS_MAX_TREELIST_PER_CHAIN */
+                                  only), at most BBS_MAX_TREELIST_PER_CHAIN;
+                                  single-dataset contexts (a batch keeps the
+                                  best only) */
   uint64_t seed; /* Philox key for moves and random initial trees */
   /* Extensions without a counterpart in the reference (defaults reproduce
    * it): the score and the error-rate move taken with probability
@@ -219,7 +221,7 @@ BBS_API int bbs_last_run_ms(const bbs_ctx *ctx, float *ms);
 
 /* get_best_am/dm/beta/score, src/Application.hpp:224-256; also the parent
  * vector, the class totals (n00,n01,n10,n11) and the chain index.  Any
- * output pointer may be NULL.  The best proposal is judged by the
+ * output pointer may be NULL.  The best proposal is chosen by the
  * reference's max score also when chains sample the sum score (whose
  * class totals are then not recorded: counts are zero). */
 BBS_API int bbs_get_best(bbs_ctx *ctx, uint64_t *am, uint64_t *dm, uint32_t *parent,
