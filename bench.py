@@ -554,16 +554,29 @@ def run_beyond_caps(N, chains, steps, flush, torch):
     return out
 
 
+def own_gpu(local: int) -> str:
+    """Makes this rank's GPU the only visible one, before any CUDA call, so
+    that torch and the library (which links its own CUDA runtime) both use
+    it as device 0.  Returns the GPU's index for nvidia-smi."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    ids = [v for v in vis.split(",") if v.strip()] if vis else []
+    gpu = ids[local] if local < len(ids) else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = gpu
+    return gpu
+
+
 def run_ours(args) -> None:
+    ws, rank, local = dist_info()
+    gpu = own_gpu(local) if ws > 1 else str(local)
+
     import numpy as np
     import torch
 
     from bbscite_gb300 import native as N
 
-    ws, rank, local = dist_info()
     if not torch.cuda.is_available():
         raise SystemExit("bench.py needs a CUDA GPU")
-    torch.cuda.set_device(local)
+    torch.cuda.set_device(0 if ws > 1 else local)
     dist = None
     if ws > 1:
         import torch.distributed as dist
@@ -612,7 +625,7 @@ def run_ours(args) -> None:
     for _ in range(args.warmup):
         bt.run(L)
         ctx.run(L)
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(gpu)
     clocks.start()
     adj_ms, adj_wall, adj_list = _timed(lambda: bt.run(L), bt.last_run_ms,
                                         args.steps, flush, barrier, torch)

@@ -56,3 +56,17 @@ def test_single_process_passthrough():
     import bench
     assert bench.max_over_ranks(None, [3, 4.5], "cpu") == [3.0, 4.5]
     assert bench.global_best(None, -2.0, 0, 1, "cpu") == (-2.0, 0)
+
+
+def test_each_rank_sees_only_its_gpu(monkeypatch):
+    """Under torchrun each rank restricts the visible GPUs to its own (the
+    library links its own CUDA runtime, so torch's device choice would not
+    reach it)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "4,5,6,7")
+    assert bench.own_gpu(2) == "6"
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "6"
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES")
+    assert bench.own_gpu(3) == "3"
+    assert os.environ["CUDA_VISIBLE_DEVICES"] == "3"
