@@ -605,12 +605,13 @@ inline constexpr float kScoreScale = 65536.0f;  // 2^16, scores: a cell's
   // |log-likelihood| stays below 2^15 for any float alpha, beta (at most
   // 255 genes of |log p| <= 104), so each cell's term fits in 32 bits
 
-// An int64 fixed-point total as a float (hi * 2^32 + lo, one rounding of
-// each part and of their sum; no double-precision arithmetic).
+// An int64 fixed-point total as a float without double-precision
+// arithmetic: x = hi * 2^24 + lo with 0 <= lo < 2^24, both exact in float
+// for |x| < 2^48, and one rounding in the fused multiply-add.
 __device__ __forceinline__ float ll_to_float(long long x) {
-  const int hi = (int)(x >> 32);
-  const unsigned lo = (unsigned)(x & 0xffffffffll);
-  return fmaf((float)hi, 4294967296.0f, __uint2float_rn(lo));
+  const int hi = (int)(x >> 24);
+  const int lo = (int)(x & 0xFFFFFFll);
+  return fmaf((float)hi, 16777216.0f, (float)lo);
 }
 inline constexpr float kLog2E = 1.44269504088896341f;
 inline constexpr float kLn2 = 0.693147180559945309f;

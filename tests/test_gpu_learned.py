@@ -267,3 +267,31 @@ def test_langevin_learns_alpha(native):
     assert abs(np.median(st["beta"]) - 0.2) < 0.06
     acc = st["err_stats"][:, 1].sum() / max(1, st["err_stats"][:, 0].sum())
     assert 0.2 < acc < 0.98
+
+
+@pytest.mark.parametrize("G,Cn,alpha,beta,score", [
+    (255, 64, 1e-30, 0.5, "sum"),     # a cell's log-likelihood near -1.8e4
+    (255, 40, 1e-3, 0.95, "sum"),     # (beta near 1 with sd 0.1 makes the
+                                      # reference's Beta prior NaN)
+    (2, 1, 1e-2, 0.3, "sum"),         # the smallest problem: moves need two
+    (2, 1, 1e-2, 0.3, "max"),         # genes (two non-root nodes)
+    (2, 3, 0.2, 0.45, "sum"),
+])
+def test_extreme_sizes_and_rates_replay_in_fp64(native, orc, G, Cn, alpha,
+                                                beta, score):
+    """Scores at the edges of the fixed-point range and of the sizes,
+    replayed step by step in FP64."""
+    m, _, _ = D.generate_dataset(7 * G + Cn, G, Cn, 1e-3, 0.2, 0.05, 0.0)
+    p = native.default_params(
+        alpha_mean=alpha, beta_mean=beta, seed=23,
+        score_mode=getattr(native, "SCORE_" + score.upper()))
+    mut, known = D.matrix_to_bits(m)
+    rng = np.random.default_rng(12)
+    starts = np.stack([D.random_parent_vector(rng, G) for _ in range(2)])
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(2, starts)
+        tr = c.run(60, trace=True)
+        final = c.chains()
+    amb = sum(replay(orc, native, m, p, starts[ch], tr[ch], final["dm"][ch])
+              for ch in range(2))
+    assert amb <= 2
