@@ -494,6 +494,8 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
         return r[len(r) // 2] if seeds % 2 else \
             0.5 * (r[seeds // 2 - 1] + r[seeds // 2])
     ratios = {a: median_ratio(a) for a in arms if a != "random_walk"}
+    # never reached within the run: null in the JSON line (not Infinity)
+    ratios = {a: (None if math.isinf(v) else v) for a, v in ratios.items()}
     return {
         "chains": chains, "steps": total, "seeds": seeds,
         "error_step": error_step, "n_genes": G, "n_cells": Cn,
@@ -504,7 +506,8 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
                      else "random_walk"} for a, (m, e) in arms.items()},
         "per_seed": per_seed,
         "median_step_ratio_over_rw": ratios,
-        "target_half_met": ratios["langevin"] <= 0.5,
+        "target_half_met": ratios["langevin"] is not None
+        and ratios["langevin"] <= 0.5,
         "rates_settle_steps": {a: [r["settle"] for r in res[a]] for a in arms},
         "error_move_acceptance": {a: [round(r["accept"], 3) for r in res[a]]
                                   for a in arms},
