@@ -84,7 +84,7 @@ def parse_args(argv=None):
                          "merge_rows")
     ap.add_argument("--mix-datasets", type=int, default=512)
     ap.add_argument("--mix-steps", type=int, default=1000)
-    ap.add_argument("--lvr-steps", type=int, default=500000,
+    ap.add_argument("--lvr-steps", type=int, default=400000,
                     help="Langevin vs random walk: steps per chain (0: off)")
     ap.add_argument("--lvr-seeds", type=int, default=4)
     ap.add_argument("--lvr-chains", type=int, default=256)
@@ -424,23 +424,29 @@ def _logit(x):
 def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
                        error_step, data_alpha, data_beta):
     """Steps-to-best of the adjoint-driven Langevin error-rate chain (sum
-    score) against the random-walk error-rate chain (the reference's max
-    score), both from alpha=1e-2, beta=0.3 with error-move probability 0.1,
-    over `seeds` independent seeds (the same Philox seeds in both arms).
-    At every checkpoint (1,000-step chunks to 20,000 steps, then
-    10,000-step chunks) each arm's best tree is scored with the reference's
-    max score at the generator's rates (a scale common to both arms: the
-    chains rank proposals at their own sampled rates), and the median over
-    chains of logit(alpha) and logit(beta) is read.  Per seed: the first
-    step count at which the Langevin arm's best is within 0.1 nats of the
-    random-walk arm's final best, and for each arm the step count after
-    which the median rates stay within 0.25 (logit alpha) and 0.05 (logit
-    beta) of their final values."""
+    score) against random-walk error-rate chains, all from alpha=1e-2,
+    beta=0.3 with error-move probability 0.1, over `seeds` independent
+    seeds (the same Philox seeds in every arm).  Arms: the preconditioned
+    random walk on (logit alpha, logit beta) with the reference's max
+    score; the reference's own beta random walk (alpha stays at its
+    start); Langevin with the sum score; Langevin with the max score.  At
+    every checkpoint (1,000-step chunks to 20,000 steps, then 10,000-step
+    chunks) each arm's best tree is scored with the reference's max score
+    at the generator's rates (a scale common to all arms: the chains rank
+    proposals at their own rates), and the median over chains of
+    logit(alpha) and logit(beta) is read.  Per seed: the first step count
+    at which each arm is within 0.1 nats of a random-walk arm's final
+    best, and the step count after which each arm's median rates stay
+    within 0.25 (logit alpha) and 0.05 (logit beta) of their final
+    values."""
     import numpy as np
 
     arms = {"random_walk": (N.SCORE_MAX, N.ERROR_RANDOM_WALK),
             "langevin": (N.SCORE_SUM, N.ERROR_LANGEVIN),
-            "langevin_max_score": (N.SCORE_MAX, N.ERROR_LANGEVIN)}
+            "langevin_max_score": (N.SCORE_MAX, N.ERROR_LANGEVIN),
+            # the reference's own chain: its beta random walk (ChangeBeta,
+            # src/MutationTree.hpp:345-351), alpha fixed at its start
+            "reference_beta_walk": (N.SCORE_MAX, N.ERROR_BETA_WALK)}
     marks = list(range(1000, 20001, 1000)) + \
         list(range(30000, total + 1, 10000))
     res = {a: [] for a in arms}
@@ -476,26 +482,35 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
                 res[name].append({"best": best, "own": own[-1],
                                   "settle": settle,
                                   "accept": float(e[1]) / max(1, int(e[0]))})
-    per_seed = []
-    for sd in range(seeds):
-        target = res["random_walk"][sd]["best"][-1] - 0.1
-        reach = {a: next((marks[k] for k, v in enumerate(res[a][sd]["best"])
-                          if v >= target), None) for a in arms}
-        per_seed.append({
-            "best": {a: res[a][sd]["best"][-1] for a in arms},
-            "steps_to_rw_best": reach,
-            "best_at_own_rates": {a: res[a][sd]["own"] for a in arms}})
+    def steps_to(arm, sd, base):
+        """First checkpoint of `arm` within 0.1 nats of `base`'s final
+        best, or None."""
+        target = res[base][sd]["best"][-1] - 0.1
+        return next((marks[k] for k, v in enumerate(res[arm][sd]["best"])
+                     if v >= target), None)
 
-    def median_ratio(arm):
-        r = sorted(p["steps_to_rw_best"][arm] /
-                   p["steps_to_rw_best"]["random_walk"]
-                   if p["steps_to_rw_best"][arm] is not None else math.inf
-                   for p in per_seed)
-        return r[len(r) // 2] if seeds % 2 else \
+    def median_ratio(arm, base):
+        r = []
+        for sd in range(seeds):
+            a, b = steps_to(arm, sd, base), steps_to(base, sd, base)
+            r.append(a / b if a is not None else math.inf)
+        r.sort()
+        med = r[len(r) // 2] if seeds % 2 else \
             0.5 * (r[seeds // 2 - 1] + r[seeds // 2])
-    ratios = {a: median_ratio(a) for a in arms if a != "random_walk"}
-    # never reached within the run: null in the JSON line (not Infinity)
-    ratios = {a: (None if math.isinf(v) else v) for a, v in ratios.items()}
+        # never reached within the run: null in the JSON line
+        return None if math.isinf(med) else med
+
+    per_seed = [{"best": {a: res[a][sd]["best"][-1] for a in arms},
+                 "steps_to_rw_best": {a: steps_to(a, sd, "random_walk")
+                                      for a in arms},
+                 "steps_to_reference_best": {
+                     a: steps_to(a, sd, "reference_beta_walk") for a in arms},
+                 "best_at_own_rates": {a: res[a][sd]["own"] for a in arms}}
+                for sd in range(seeds)]
+    ratios = {a: median_ratio(a, "random_walk") for a in arms
+              if a not in ("random_walk", "reference_beta_walk")}
+    ratios_ref = {a: median_ratio(a, "reference_beta_walk") for a in arms
+                  if a not in ("random_walk", "reference_beta_walk")}
     return {
         "chains": chains, "steps": total, "seeds": seeds,
         "error_step": error_step, "n_genes": G, "n_cells": Cn,
@@ -506,8 +521,11 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
                      else "random_walk"} for a, (m, e) in arms.items()},
         "per_seed": per_seed,
         "median_step_ratio_over_rw": ratios,
+        "median_step_ratio_over_reference_beta_walk": ratios_ref,
         "target_half_met": ratios["langevin"] is not None
         and ratios["langevin"] <= 0.5,
+        "target_half_met_vs_reference_beta_walk":
+            ratios_ref["langevin"] is not None and ratios_ref["langevin"] <= 0.5,
         "rates_settle_steps": {a: [r["settle"] for r in res[a]] for a in arms},
         "error_move_acceptance": {a: [round(r["accept"], 3) for r in res[a]]
                                   for a in arms},
