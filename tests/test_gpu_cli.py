@@ -120,3 +120,31 @@ def test_cpp_tree_scorer_kat(probe, kat, orc):
             * math.log(1 - b) + t["log(beta)"] * math.log(b)
             + t["log(alpha)"] * math.log(a) + want_prior)
     assert score == pytest.approx(want, rel=k["catch_approx_rel"])
+
+
+def test_cli_application_kat(native, orc, kat, tmp_path):
+    """The reference's end-to-end test (test/Application.cpp:38-143)
+    through the command line: the tree in _ml0 scores like the true tree
+    under the reference's scorer."""
+    from bbscite_gb300 import build as B
+    k = kat["application"]
+    G, Cn = k["n_genes"], k["n_cells"]
+    m = np.array([[(int(k["is_mutated"][c], 2) >> g) & 1 for c in range(Cn)]
+                  for g in range(G)], dtype=np.int8)
+    D.write_csv(m, str(tmp_path / "app.csv"))
+    r = subprocess.run([B.CLI, "-i", "app.csv", "-r", str(k["n_chains"]),
+                        "-l", str(k["chain_length"]), "-fd", str(k["alpha"]),
+                        "-ad", str(k["beta"]), "-sd", str(k["beta_sd"]),
+                        "-seed", "1"], cwd=tmp_path, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    from bbscite_gb300.verification import lib as L
+    found = L.parse_newick((tmp_path / "app_ml0.newick").read_text())
+    mut, known = D.matrix_to_bits(m)
+    _, dm_found = orc.parent_to_matrix(found)
+    _, dm_true = orc.parent_to_matrix(np.array(k["true_parent_vector"]))
+    s_found = orc.logscore_tree(k["alpha"], k["beta"], k["beta_sd"], dm_found,
+                                mut, known, k["beta"])[0]
+    s_true = orc.logscore_tree(k["alpha"], k["beta"], k["beta_sd"], dm_true,
+                               mut, known, k["beta"])[0]
+    assert s_found == pytest.approx(s_true, rel=1.2e-5)
