@@ -605,6 +605,18 @@ inline constexpr float kScoreScale = 65536.0f;  // 2^16, scores: a cell's
   // |log-likelihood| stays below 2^15 for any float alpha, beta (at most
   // 255 genes of |log p| <= 104), so each cell's term fits in 32 bits
 
+// The warp's sum of an int64 per lane (|x| < 2^40) with three 32-bit
+// warp reductions: the high word and two 16-bit pieces of the low word,
+// whose 32-lane sums cannot overflow; the same total in every lane.
+__device__ __forceinline__ long long warp_sum_ll(long long x) {
+  const int hi = (int)(x >> 32);
+  const unsigned lo = (unsigned)(x & 0xFFFFFFFFll);
+  const long long h = (long long)__reduce_add_sync(BBS_FULL_MASK, hi);
+  const long long m = (long long)__reduce_add_sync(BBS_FULL_MASK, lo >> 16);
+  const long long l = (long long)__reduce_add_sync(BBS_FULL_MASK, lo & 0xFFFFu);
+  return h * 4294967296ll + m * 65536ll + l;
+}
+
 // An int64 fixed-point total as a float without double-precision
 // arithmetic: x = hi * 2^24 + lo with 0 <= lo < 2^24, both exact in float
 // for |x| < 2^48, and one rounding in the fused multiply-add.
@@ -747,9 +759,7 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
     }
   }
 #pragma unroll
-  for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-    for (int i = 0; i < 6; i++) acc[i] += __shfl_xor_sync(BBS_FULL_MASK, acc[i], off);
+  for (int i = 0; i < 6; i++) acc[i] = warp_sum_ll(acc[i]);
 }
 
 // Class totals (n00, n01, n10, n11) from the sums.

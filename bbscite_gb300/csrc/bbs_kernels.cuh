@@ -372,6 +372,29 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   }
 }
 
+// One work unit of the batched launch: chain `chain` of dataset `d`.
+template <int W32, int Q, bool SUM>
+__device__ __forceinline__ void batch_unit(const BatchArgs &b,
+                                           const DatasetDev &ds,
+                                           const ModelDev &md, uint32_t chain,
+                                           uint32_t d, uint32_t *buf0,
+                                           int *part, volatile int *sflag,
+                                           Cells<W32, Q> &cb, int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  // the dataset's node count is within this launch's row width
+  uint32_t *buf1 = buf0 + ds.n_nodes * RS;
+  const bool resident = ds.n_cells <= 32 * Q;
+  if (resident) load_cells<W32, Q>(cb, ds, 0, 32, lane);
+  const uint64_t off = b.chain_off[chain];
+  // Philox key: the chain's number within its dataset, so a dataset's
+  // chains draw the same moves here as in a one-dataset run.
+  const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
+  run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
+                         nullptr, nullptr, 1, b.states + chain, nullptr,
+                         nullptr, b.n_steps, b.cancel, b.status, buf0, buf1,
+                         part, sflag, cb, resident, 1, 0, lane);
+}
+
 // Many datasets: warps take chains from a shared work list (costliest
 // first); each chain brings its own dataset and rules.  One warp per chain.
 template <int W32, int Q, bool SUM>
@@ -382,7 +405,6 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   uint32_t *buf0 = smem + (size_t)wib * slot_words(b.max_nodes, RS, 1);
-  uint32_t *buf1 = buf0 + b.max_nodes * RS;
   int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
   volatile int *sflag = part + 24;
   Cells<W32, Q> cb;
@@ -393,21 +415,18 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
     if (unit >= (unsigned int)b.n_units) break;
     const uint32_t chain = b.units[unit];
     const uint32_t d = b.chain_ds[chain];
-    const DatasetDev ds = b.ds[d];
-    const ModelDev md = b.md[d];
-    // the dataset's node count is within this launch's row width
-    uint32_t *buf1d = buf0 + ds.n_nodes * RS;
-    const bool resident = ds.n_cells <= 32 * Q;
-    if (resident) load_cells<W32, Q>(cb, ds, 0, 32, lane);
-    const uint64_t off = b.chain_off[chain];
-    // Philox key: the chain's number within its dataset, so a dataset's
-    // chains draw the same moves here as in a one-dataset run.
-    const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
-    run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
-                           nullptr, nullptr, 1, b.states + chain, nullptr, nullptr, b.n_steps,
-                           b.cancel, b.status, buf0, buf1d, part, sflag, cb,
-                           resident, 1, 0, lane);
-    (void)buf1;
+    // The sum score reads the dataset and model tables in place (fewer
+    // registers, measured faster); the max score keeps register copies
+    // (measured faster there).
+    if constexpr (SUM) {
+      batch_unit<W32, Q, SUM>(b, b.ds[d], b.md[d], chain, d, buf0, part,
+                              sflag, cb, lane);
+    } else {
+      const DatasetDev ds = b.ds[d];
+      const ModelDev md = b.md[d];
+      batch_unit<W32, Q, SUM>(b, ds, md, chain, d, buf0, part, sflag, cb,
+                              lane);
+    }
   }
 }
 
