@@ -89,7 +89,7 @@ def parse_args(argv=None):
     ap.add_argument("--lvr-seeds", type=int, default=4)
     ap.add_argument("--lvr-chains", type=int, default=256)
     ap.add_argument("--lvr-error-step", type=float, default=1.2)
-    ap.add_argument("--caps-steps", type=int, default=200,
+    ap.add_argument("--caps-steps", type=int, default=500,
                     help="255x512 run: steps per launch (0: off)")
     ap.add_argument("--caps-chains", type=int, default=4096)
     return ap.parse_args(argv)
@@ -532,11 +532,14 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     }
 
 
-def run_beyond_caps(N, chains, steps, flush, torch):
+def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
     """255 genes x 512 cells (alpha=5e-4, beta=0.25, 8% unknown, 1%
     homozygous): the batched form with the sum score and Langevin error
     moves against the plain form (max score, fixed rates), device time of
-    one launch of `steps` steps after a warm-up launch."""
+    one launch of `steps` steps after `warm` warm-up steps (the rate of the
+    first few hundred steps from random trees is lower: the sum score sums
+    many cells twice while their best attachment lies far below the bound
+    it is taken against)."""
     from bbscite_gb300 import data as D
     G, Cn = 255, 512
     m, _, _ = D.generate_dataset(5255, G, Cn, 5e-4, 0.25, 0.08, 0.01)
@@ -545,11 +548,12 @@ def run_beyond_caps(N, chains, steps, flush, torch):
                            prob_beta_change=0.1, score_mode=N.SCORE_SUM,
                            error_move=N.ERROR_LANGEVIN)
     plain = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5)
-    out = {"n_genes": G, "n_cells": Cn, "chains": chains, "steps": steps}
+    out = {"n_genes": G, "n_cells": Cn, "chains": chains, "steps": steps,
+           "warm_up_steps": warm}
     with N.Batch([(mut, known, Cn, G)], adj) as bt:
         bt.init_chains(chains)
         bt.autotune(max(8, steps // 10))
-        bt.run(steps)
+        bt.run(warm)
         flush.zero_()
         torch.cuda.synchronize()
         bt.run(steps)
@@ -559,7 +563,7 @@ def run_beyond_caps(N, chains, steps, flush, torch):
     with N.Context(mut, known, Cn, G, plain) as c:
         c.init_chains(chains)
         c.autotune(max(8, steps // 10))
-        c.run(steps)
+        c.run(warm)
         flush.zero_()
         torch.cuda.synchronize()
         c.run(steps)
