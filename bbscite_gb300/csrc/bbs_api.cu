@@ -235,6 +235,10 @@ struct bbs_ctx {
   bool running = false;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.0f;
+  // scratch of the host-buffer scoring calls and its pinned host mirror,
+  // scratch_cap bytes each; grows, never shrinks
+  uint8_t *d_scratch = nullptr, *h_scratch = nullptr;
+  size_t scratch_cap = 0;
 };
 
 namespace {
@@ -372,6 +376,81 @@ struct DevBuf {
   T *p = nullptr;
   ~DevBuf() { cudaFree(p); }
   cudaError_t alloc(size_t n) { return cudaMalloc((void **)&p, sizeof(T) * std::max<size_t>(n, 1)); }
+};
+
+// A piece of the context's scratch: its device address and the same
+// offset in the pinned host mirror.
+template <typename T>
+struct Piece {
+  T *d;
+  T *h;
+};
+
+// Pieces of the context's scratch for one call of a host-buffer entry point
+// (bbs_score_trees, bbs_apply_moves, bbs_sumscore_grad).  The call adds up
+// its pieces with add(), reserves once, then takes them in the same order
+// with take(); inputs come first and outputs last, so that each call moves
+// one contiguous range each way between the pinned mirror and the device.
+// The scratch only moves while nothing is taken, and a caller that scores
+// one tree at a time allocates on its first call only.
+class ScratchPlan {
+ public:
+  template <typename T>
+  void add(size_t n) { bytes_ += piece(sizeof(T) * n); }
+  int reserve(bbs_ctx *c) {
+    c_ = c;
+    off_ = 0;
+    if (bytes_ <= c->scratch_cap) return BBS_OK;
+    // every entry point drains the stream before it returns, so no copy or
+    // kernel of an earlier call still uses the old scratch
+    cudaFree(c->d_scratch);
+    if (c->h_scratch) cudaFreeHost(c->h_scratch);
+    c->d_scratch = c->h_scratch = nullptr;
+    c->scratch_cap = 0;
+    // half again as much, so that a slowly growing caller reallocates
+    // rarely; the exact size when that much is not free
+    for (const size_t cap : {bytes_ + bytes_ / 2, bytes_}) {
+      cudaError_t e = cudaMalloc(&c->d_scratch, cap);
+      if (e == cudaSuccess) e = cudaHostAlloc(&c->h_scratch, cap, cudaHostAllocDefault);
+      if (e == cudaSuccess) {
+        c->scratch_cap = cap;
+        return BBS_OK;
+      }
+      (void)cudaGetLastError();
+      cudaFree(c->d_scratch);
+      if (c->h_scratch) cudaFreeHost(c->h_scratch);
+      c->d_scratch = c->h_scratch = nullptr;
+      if (cap == bytes_) return cuda_fail((int)e, "scratch allocation");
+    }
+    return BBS_OK;
+  }
+  template <typename T>
+  Piece<T> take(size_t n) {
+    Piece<T> p{reinterpret_cast<T *>(c_->d_scratch + off_),
+               reinterpret_cast<T *>(c_->h_scratch + off_)};
+    off_ += piece(sizeof(T) * n);
+    return p;
+  }
+  // Offset of the next piece: the end of the inputs, the start of the outputs.
+  size_t mark() const { return off_; }
+  // One copy of the mirror's bytes [from, to) to the device or back, on the
+  // context's stream.
+  cudaError_t to_device(size_t from, size_t to) const {
+    return cudaMemcpyAsync(c_->d_scratch + from, c_->h_scratch + from, to - from,
+                           cudaMemcpyHostToDevice, c_->stream);
+  }
+  cudaError_t to_host(size_t from, size_t to) const {
+    return cudaMemcpyAsync(c_->h_scratch + from, c_->d_scratch + from, to - from,
+                           cudaMemcpyDeviceToHost, c_->stream);
+  }
+
+ private:
+  // 256-byte aligned; an empty piece takes no room, so a piece that add()
+  // left out may still be taken with n = 0
+  static size_t piece(size_t bytes) { return (bytes + 255) & ~size_t(255); }
+  bbs_ctx *c_ = nullptr;
+  size_t bytes_ = 0;
+  size_t off_ = 0;
 };
 
 }  // namespace
@@ -615,6 +694,8 @@ void bbs_destroy(bbs_ctx *c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_chains(c);
+  cudaFree(c->d_scratch);
+  if (c->h_scratch) cudaFreeHost(c->h_scratch);
   cudaFree(c->d_K);
   cudaFree(c->d_M);
   cudaFree(c->d_ds);
@@ -638,34 +719,6 @@ int bbs_get_sizes(const bbs_ctx *c, uint32_t *n_cells, uint32_t *n_genes,
 }
 
 namespace {
-
-// Scores trees already on the device; optionally initialises chain states.
-int score_device(bbs_ctx *c, const uint32_t *d_rows, const float *betas,
-                 uint32_t n_trees, float *d_scores, uint64_t *d_counts,
-                 uint32_t *d_attach, ChainState *d_states) {
-  std::vector<float> terms(4 * (size_t)n_trees);
-  for (uint32_t t = 0; t < n_trees; t++) {
-    terms[4 * t] = betas[t];
-    host_beta_terms(c->ds, betas[t], &terms[4 * t + 1], &terms[4 * t + 2],
-                    &terms[4 * t + 3]);
-  }
-  DevBuf<float> d_terms;
-  BBS_CUDA(d_terms.alloc(terms.size()), "cudaMalloc");
-  BBS_CUDA(cudaMemcpyAsync(d_terms.p, terms.data(), sizeof(float) * terms.size(),
-                           cudaMemcpyHostToDevice, c->stream), "cudaMemcpy");
-  ScoreArgs a{};
-  a.ds = c->ds;
-  a.rows = d_rows;
-  a.beta_terms = d_terms.p;
-  a.n_trees = (int)n_trees;
-  a.scores = d_scores;
-  a.counts = d_counts;
-  a.attach = d_attach;
-  a.states = d_states;
-  const int e = launch_score(a, c->q, c->stream);
-  if (e != 0) return cuda_fail(e, "score kernel launch");
-  return sync_stream(c, "score kernel");
-}
 
 // Launch shape without timing: split the cells over up to four warps per
 // chain when there are too few chains to give every scheduler ~3 warps,
@@ -694,15 +747,8 @@ void default_launch(bbs_ctx *c) {
   c->cpb = c->wpc == 1 ? (c->n_chains >= (uint32_t)c->n_sms * 16 ? 4 : 1) : 1;
 }
 
-int upload_trees(bbs_ctx *c, const uint64_t *dm, uint32_t n_trees,
-                 uint32_t **d_out) {
-  const size_t words = (size_t)n_trees * c->n_nodes * c->W64;
-  cudaError_t e = cudaMalloc(d_out, sizeof(uint64_t) * std::max<size_t>(words, 1));
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(*d_out, dm, sizeof(uint64_t) * words,
-                        cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return cuda_fail((int)e, "tree upload");
-  return BBS_OK;
+size_t tree_words(const bbs_ctx *c, uint32_t n_trees) {
+  return (size_t)n_trees * c->n_nodes * c->W64;
 }
 
 }  // namespace
@@ -1147,29 +1193,48 @@ int bbs_score_trees(bbs_ctx *c, const uint64_t *dm, const float *betas,
     for (uint32_t t = 0; t < n_trees; t++)
       if (!(betas[t] > 0.0f && betas[t] < 1.0f))
         return fail(BBS_ERR_INPUT, "beta of tree %u outside (0, 1)", t);
-    uint32_t *d_rows = nullptr;
-    int r = upload_trees(c, dm, n_trees, &d_rows);
+    const size_t words = tree_words(c, n_trees);
+    const size_t n_attach = (size_t)n_trees * c->n_cells;
+    ScratchPlan plan;
+    plan.add<uint64_t>(words);
+    plan.add<float>(4 * (size_t)n_trees);
+    plan.add<float>(n_trees);
+    if (counts) plan.add<uint64_t>(4 * (size_t)n_trees);
+    if (attach) plan.add<uint32_t>(n_attach);
+    int r = plan.reserve(c);
     if (r != BBS_OK) return r;
-    DevBuf<uint32_t> rows_guard;
-    rows_guard.p = d_rows;
-    DevBuf<float> d_scores;
-    DevBuf<uint64_t> d_counts;
-    DevBuf<uint32_t> d_attach;
-    BBS_CUDA(d_scores.alloc(n_trees), "cudaMalloc");
-    if (counts) BBS_CUDA(d_counts.alloc(4 * (size_t)n_trees), "cudaMalloc");
-    if (attach) BBS_CUDA(d_attach.alloc((size_t)n_trees * c->n_cells), "cudaMalloc");
-    r = score_device(c, d_rows, betas, n_trees, d_scores.p, d_counts.p,
-                     d_attach.p, nullptr);
+    const auto rows = plan.take<uint64_t>(words);
+    const auto terms = plan.take<float>(4 * (size_t)n_trees);
+    const size_t out_begin = plan.mark();
+    const auto d_scores = plan.take<float>(n_trees);
+    const auto d_counts = plan.take<uint64_t>(counts ? 4 * (size_t)n_trees : 0);
+    const auto d_attach = plan.take<uint32_t>(attach ? n_attach : 0);
+    const size_t out_end = plan.mark();
+    // inputs: the ancestor rows and the host log-table terms of each beta
+    std::memcpy(rows.h, dm, sizeof(uint64_t) * words);
+    for (uint32_t t = 0; t < n_trees; t++) {
+      float *tt = terms.h + 4 * (size_t)t;
+      tt[0] = betas[t];
+      host_beta_terms(c->ds, betas[t], &tt[1], &tt[2], &tt[3]);
+    }
+    BBS_CUDA(plan.to_device(0, out_begin), "scratch upload");
+    ScoreArgs a{};
+    a.ds = c->ds;
+    a.rows = reinterpret_cast<const uint32_t *>(rows.d);
+    a.beta_terms = terms.d;
+    a.n_trees = (int)n_trees;
+    a.scores = d_scores.d;
+    a.counts = counts ? d_counts.d : nullptr;
+    a.attach = attach ? d_attach.d : nullptr;
+    a.states = nullptr;
+    const int e = launch_score(a, c->q, c->stream);
+    if (e != 0) return cuda_fail(e, "score kernel launch");
+    BBS_CUDA(plan.to_host(out_begin, out_end), "result copy");
+    r = sync_stream(c, "score kernel");
     if (r != BBS_OK) return r;
-    BBS_CUDA(cudaMemcpy(scores, d_scores.p, sizeof(float) * n_trees,
-                        cudaMemcpyDeviceToHost), "copy");
-    if (counts)
-      BBS_CUDA(cudaMemcpy(counts, d_counts.p, sizeof(uint64_t) * 4 * n_trees,
-                          cudaMemcpyDeviceToHost), "copy");
-    if (attach)
-      BBS_CUDA(cudaMemcpy(attach, d_attach.p,
-                          sizeof(uint32_t) * (size_t)n_trees * c->n_cells,
-                          cudaMemcpyDeviceToHost), "copy");
+    std::memcpy(scores, d_scores.h, sizeof(float) * n_trees);
+    if (counts) std::memcpy(counts, d_counts.h, sizeof(uint64_t) * 4 * n_trees);
+    if (attach) std::memcpy(attach, d_attach.h, sizeof(uint32_t) * n_attach);
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_score_trees");
@@ -1205,54 +1270,55 @@ int bbs_apply_moves(bbs_ctx *c, const uint64_t *dm, const float *betas,
           return fail(BBS_ERR_INPUT, "move %u names a node >= %u", t, n);
       }
     }
-    uint32_t *d_rows = nullptr;
-    int r = upload_trees(c, dm, n_trees, &d_rows);
+    const size_t words = tree_words(c, n_trees);
+    ScratchPlan plan;
+    plan.add<uint64_t>(words);
+    plan.add<float>(n_trees);
+    if (raw)
+      plan.add<bbs_raw_move>(n_trees);
+    else
+      plan.add<bbs_move_params>(n_trees);
+    plan.add<uint64_t>(words);
+    plan.add<float>(n_trees);
+    plan.add<bbs_move_params>(n_trees);
+    int r = plan.reserve(c);
     if (r != BBS_OK) return r;
-    DevBuf<uint32_t> rows_guard;
-    rows_guard.p = d_rows;
-    const size_t words = (size_t)n_trees * n * c->W64;
-    DevBuf<uint64_t> d_out;
-    DevBuf<float> d_betas, d_bout;
-    DevBuf<bbs_raw_move> d_raw;
-    DevBuf<bbs_move_params> d_par, d_pout;
-    BBS_CUDA(d_out.alloc(words), "cudaMalloc");
-    BBS_CUDA(d_betas.alloc(n_trees), "cudaMalloc");
-    BBS_CUDA(d_bout.alloc(n_trees), "cudaMalloc");
-    BBS_CUDA(d_pout.alloc(n_trees), "cudaMalloc");
-    BBS_CUDA(cudaMemcpyAsync(d_betas.p, betas, sizeof(float) * n_trees,
-                             cudaMemcpyHostToDevice, c->stream), "copy");
-    if (raw) {
-      BBS_CUDA(d_raw.alloc(n_trees), "cudaMalloc");
-      BBS_CUDA(cudaMemcpyAsync(d_raw.p, raw, sizeof(bbs_raw_move) * n_trees,
-                               cudaMemcpyHostToDevice, c->stream), "copy");
-    } else {
-      BBS_CUDA(d_par.alloc(n_trees), "cudaMalloc");
-      BBS_CUDA(cudaMemcpyAsync(d_par.p, params, sizeof(bbs_move_params) * n_trees,
-                               cudaMemcpyHostToDevice, c->stream), "copy");
-    }
-    BBS_CUDA(cudaMemsetAsync(d_out.p, 0, sizeof(uint64_t) * words, c->stream), "memset");
+    const auto rows = plan.take<uint64_t>(words);
+    const auto in_betas = plan.take<float>(n_trees);
+    const auto in_raw = plan.take<bbs_raw_move>(raw ? n_trees : 0);
+    const auto in_par = plan.take<bbs_move_params>(raw ? 0 : n_trees);
+    const size_t out_begin = plan.mark();
+    const auto out_rows = plan.take<uint64_t>(words);
+    const auto out_beta = plan.take<float>(n_trees);
+    const auto out_par = plan.take<bbs_move_params>(n_trees);
+    const size_t out_end = plan.mark();
+    std::memcpy(rows.h, dm, sizeof(uint64_t) * words);
+    std::memcpy(in_betas.h, betas, sizeof(float) * n_trees);
+    if (raw)
+      std::memcpy(in_raw.h, raw, sizeof(bbs_raw_move) * n_trees);
+    else
+      std::memcpy(in_par.h, params, sizeof(bbs_move_params) * n_trees);
+    BBS_CUDA(plan.to_device(0, out_begin), "scratch upload");
+    BBS_CUDA(cudaMemsetAsync(out_rows.d, 0, sizeof(uint64_t) * words, c->stream), "memset");
     ApplyArgs a{};
     a.n_nodes = (int)n;
     a.n_trees = (int)n_trees;
-    a.rows = d_rows;
-    a.betas = d_betas.p;
-    a.raw = d_raw.p;
-    a.params = d_par.p;
-    a.params_out = d_pout.p;
-    a.rows_out = (uint32_t *)d_out.p;
-    a.beta_out = d_bout.p;
+    a.rows = reinterpret_cast<const uint32_t *>(rows.d);
+    a.betas = in_betas.d;
+    a.raw = raw ? in_raw.d : nullptr;
+    a.params = raw ? nullptr : in_par.d;
+    a.params_out = out_par.d;
+    a.rows_out = reinterpret_cast<uint32_t *>(out_rows.d);
+    a.beta_out = out_beta.d;
     const int e = launch_apply(a, c->stream);
     if (e != 0) return cuda_fail(e, "apply kernel launch");
+    BBS_CUDA(plan.to_host(out_begin, out_end), "result copy");
     r = sync_stream(c, "apply kernel");
     if (r != BBS_OK) return r;
-    BBS_CUDA(cudaMemcpy(dm_out, d_out.p, sizeof(uint64_t) * words,
-                        cudaMemcpyDeviceToHost), "copy");
-    if (beta_out)
-      BBS_CUDA(cudaMemcpy(beta_out, d_bout.p, sizeof(float) * n_trees,
-                          cudaMemcpyDeviceToHost), "copy");
+    std::memcpy(dm_out, out_rows.h, sizeof(uint64_t) * words);
+    if (beta_out) std::memcpy(beta_out, out_beta.h, sizeof(float) * n_trees);
     if (params_out)
-      BBS_CUDA(cudaMemcpy(params_out, d_pout.p, sizeof(bbs_move_params) * n_trees,
-                          cudaMemcpyDeviceToHost), "copy");
+      std::memcpy(params_out, out_par.h, sizeof(bbs_move_params) * n_trees);
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_apply_moves");
@@ -1266,54 +1332,57 @@ int bbs_sumscore_grad(bbs_ctx *c, const uint64_t *dm, const float *alphas,
     if (!c || !dm || !alphas || !betas || !logl)
       return fail(BBS_ERR_INPUT, "NULL argument");
     if (n_trees == 0) return BBS_OK;
-    std::vector<float> tab(6 * (size_t)n_trees);
     for (uint32_t t = 0; t < n_trees; t++) {
       const double a = alphas[t], b = betas[t];
       if (!(a > 0 && a < 1 && b > 0 && b < 1))
         return fail(BBS_ERR_INPUT, "error rates of tree %u outside (0, 1)", t);
-      float *r = &tab[6 * t];
-      r[0] = alphas[t];
-      r[1] = betas[t];
-      r[2] = (float)std::log1p(-a);
-      r[3] = (float)std::log(b);
-      r[4] = (float)std::log(a);
-      r[5] = (float)std::log1p(-b);
     }
-    uint32_t *d_rows = nullptr;
-    int r = upload_trees(c, dm, n_trees, &d_rows);
+    const size_t words = tree_words(c, n_trees);
+    const size_t n_post = (size_t)n_trees * c->n_cells * c->n_nodes;
+    ScratchPlan plan;
+    plan.add<uint64_t>(words);
+    plan.add<float>(6 * (size_t)n_trees);
+    plan.add<float>(3 * (size_t)n_trees);
+    if (posterior) plan.add<float>(n_post);
+    int r = plan.reserve(c);
     if (r != BBS_OK) return r;
-    DevBuf<uint32_t> rows_guard;
-    rows_guard.p = d_rows;
-    DevBuf<float> d_tab, d_out, d_post;
-    BBS_CUDA(d_tab.alloc(tab.size()), "cudaMalloc");
-    BBS_CUDA(d_out.alloc(3 * (size_t)n_trees), "cudaMalloc");
-    if (posterior)
-      BBS_CUDA(d_post.alloc((size_t)n_trees * c->n_cells * c->n_nodes), "cudaMalloc");
-    BBS_CUDA(cudaMemcpyAsync(d_tab.p, tab.data(), sizeof(float) * tab.size(),
-                             cudaMemcpyHostToDevice, c->stream), "copy");
+    const auto rows = plan.take<uint64_t>(words);
+    const auto tab = plan.take<float>(6 * (size_t)n_trees);
+    const size_t out_begin = plan.mark();
+    const auto out = plan.take<float>(3 * (size_t)n_trees);
+    const auto post = plan.take<float>(posterior ? n_post : 0);
+    const size_t out_end = plan.mark();
+    std::memcpy(rows.h, dm, sizeof(uint64_t) * words);
+    // per tree: alpha, beta, log(1-alpha), log beta, log alpha, log(1-beta)
+    for (uint32_t t = 0; t < n_trees; t++) {
+      const double a = alphas[t], b = betas[t];
+      float *tt = tab.h + 6 * (size_t)t;
+      tt[0] = alphas[t];
+      tt[1] = betas[t];
+      tt[2] = (float)std::log1p(-a);
+      tt[3] = (float)std::log(b);
+      tt[4] = (float)std::log(a);
+      tt[5] = (float)std::log1p(-b);
+    }
+    BBS_CUDA(plan.to_device(0, out_begin), "scratch upload");
     GradArgs a{};
     a.ds = c->ds;
-    a.rows = d_rows;
-    a.tables = d_tab.p;
+    a.rows = reinterpret_cast<const uint32_t *>(rows.d);
+    a.tables = tab.d;
     a.n_trees = (int)n_trees;
-    a.logl = d_out.p;
-    a.dalpha = d_out.p + n_trees;
-    a.dbeta = d_out.p + 2 * (size_t)n_trees;
-    a.posterior = d_post.p;
+    a.logl = out.d;
+    a.dalpha = out.d + n_trees;
+    a.dbeta = out.d + 2 * (size_t)n_trees;
+    a.posterior = posterior ? post.d : nullptr;
     const int e = launch_grad(a, c->q, c->stream);
     if (e != 0) return cuda_fail(e, "adjoint kernel launch");
+    BBS_CUDA(plan.to_host(out_begin, out_end), "result copy");
     r = sync_stream(c, "adjoint kernel");
     if (r != BBS_OK) return r;
-    std::vector<float> out(3 * (size_t)n_trees);
-    BBS_CUDA(cudaMemcpy(out.data(), d_out.p, sizeof(float) * out.size(),
-                        cudaMemcpyDeviceToHost), "copy");
-    std::memcpy(logl, out.data(), sizeof(float) * n_trees);
-    if (dalpha) std::memcpy(dalpha, out.data() + n_trees, sizeof(float) * n_trees);
-    if (dbeta) std::memcpy(dbeta, out.data() + 2 * n_trees, sizeof(float) * n_trees);
-    if (posterior)
-      BBS_CUDA(cudaMemcpy(posterior, d_post.p,
-                          sizeof(float) * (size_t)n_trees * c->n_cells * c->n_nodes,
-                          cudaMemcpyDeviceToHost), "copy");
+    std::memcpy(logl, out.h, sizeof(float) * n_trees);
+    if (dalpha) std::memcpy(dalpha, out.h + n_trees, sizeof(float) * n_trees);
+    if (dbeta) std::memcpy(dbeta, out.h + 2 * (size_t)n_trees, sizeof(float) * n_trees);
+    if (posterior) std::memcpy(posterior, post.h, sizeof(float) * n_post);
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_sumscore_grad");

@@ -250,7 +250,11 @@ BBS_API int bbs_get_chains(bbs_ctx *ctx, uint64_t *dm, float *alpha, float *beta
  * dm = n_trees x n_nodes x W ancestor rows, betas (n_trees).  Outputs:
  * scores (class-total form: ((l00*N00 + l01*N01) + l10*N10) + l11*N11 plus
  * logscore_beta), counts (n_trees x 4, may be NULL), attach (n_trees x
- * n_cells first-max attachment nodes, may be NULL). */
+ * n_cells first-max attachment nodes, may be NULL).  This call, and
+ * bbs_apply_moves and bbs_sumscore_grad, keep their device scratch in the
+ * context: it grows to the largest call made so far and is freed by
+ * bbs_destroy, so a caller scoring one tree at a time allocates device
+ * memory on its first call only. */
 BBS_API int bbs_score_trees(bbs_ctx *ctx, const uint64_t *dm, const float *betas,
                     uint32_t n_trees, float *scores, uint64_t *counts,
                     uint32_t *attach);

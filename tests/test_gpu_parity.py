@@ -89,6 +89,53 @@ def test_score_random_shapes(native, orc, G, Cn):
             assert (counts[t] == oc).all() and (att[t] == oatt).all()
 
 
+def test_scratch_reuse_across_calls(native, orc):
+    """The host-buffer entry points keep their device scratch in the
+    context and grow it on demand: calls of mixed sizes and kinds on one
+    context give bit-for-bit the results of the same calls on a fresh
+    context, and scoring trees one at a time equals scoring them at once."""
+    G, Cn = 95, 96
+    m, _, _ = D.generate_dataset(5, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    rng = np.random.default_rng(44)
+    mp = orc.move_probs(0.1, 0.3, 0.3, 0.3)
+    calls = []
+    for n_trees in (1, 300, 7, 1000, 2):
+        dms = tree_stack(orc, [D.random_parent_vector(rng, G)
+                               for _ in range(n_trees)])
+        betas = rng.uniform(0.05, 0.6, size=n_trees).astype(np.float32)
+        raws = np.concatenate([orc.sample_moves(mp, G + 1, G, t, 1)
+                               for t in range(n_trees)])
+        calls.append((dms, betas, np.ascontiguousarray(raws).view(
+            native.RAW_MOVE)))
+
+    def run(c, dms, betas, raw):
+        s, cnt, att = c.score_trees(dms, betas, attach=True)
+        pout, out, bout = c.apply_moves(dms, betas, raw=raw)
+        logl, da, db, post = c.sumscore_grad(dms, 1e-3, betas,
+                                             posterior=len(dms) < 10)
+        return [s, cnt, att, pout.tobytes(), out, bout, logl, da, db, post]
+
+    c, _, _ = ctx_for(native, m, 1e-3, 0.2)
+    with c:
+        shared = [run(c, *call) for call in calls]
+        dms, betas, _ = calls[3]
+        one_by_one = [c.score_trees(dms[t:t + 1], betas[t:t + 1])[0][0]
+                      for t in range(50)]
+        np.testing.assert_array_equal(np.array(one_by_one, np.float32),
+                                      shared[3][0][:50])
+    for call, got in zip(calls, shared):
+        c, _, _ = ctx_for(native, m, 1e-3, 0.2)
+        with c:
+            want = run(c, *call)
+        for g, w in zip(got, want):
+            if w is None:
+                assert g is None
+            elif isinstance(w, bytes):
+                assert g == w
+            else:
+                np.testing.assert_array_equal(g, w)
+
+
 # --------------------------------------------------------------- moves --
 
 def test_apply_params_kat(native, kat):
