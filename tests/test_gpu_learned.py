@@ -276,6 +276,8 @@ def test_langevin_learns_alpha(native):
     (2, 1, 1e-2, 0.3, "sum"),         # the smallest problem: moves need two
     (2, 1, 1e-2, 0.3, "max"),         # genes (two non-root nodes)
     (2, 3, 0.2, 0.45, "sum"),
+    (255, 65535, 1e-3, 0.2, "sum"),   # the largest problem (fixed-point
+                                      # sums near 2^43 of their 2^48 range)
 ])
 def test_extreme_sizes_and_rates_replay_in_fp64(native, orc, G, Cn, alpha,
                                                 beta, score):
@@ -287,11 +289,13 @@ def test_extreme_sizes_and_rates_replay_in_fp64(native, orc, G, Cn, alpha,
         score_mode=getattr(native, "SCORE_" + score.upper()))
     mut, known = D.matrix_to_bits(m)
     rng = np.random.default_rng(12)
-    starts = np.stack([D.random_parent_vector(rng, G) for _ in range(2)])
+    # an FP64 evaluation of the largest problem takes about 0.4 s
+    chains, steps = (1, 10) if G * Cn > 10 ** 6 else (2, 60)
+    starts = np.stack([D.random_parent_vector(rng, G) for _ in range(chains)])
     with native.Context(mut, known, Cn, G, p) as c:
-        c.init_chains(2, starts)
-        tr = c.run(60, trace=True)
+        c.init_chains(chains, starts)
+        tr = c.run(steps, trace=True)
         final = c.chains()
     amb = sum(replay(orc, native, m, p, starts[ch], tr[ch], final["dm"][ch])
-              for ch in range(2))
+              for ch in range(chains))
     assert amb <= 2

@@ -266,6 +266,54 @@ def test_mcmc_replay_random(native, orc, G, Cn, chains):
     _replay_check(native, orc, m, 1e-3, 0.2, starts, raws)
 
 
+@pytest.fixture(scope="module")
+def largest():
+    """The largest problem the library takes: BBS_MAX_GENES genes and
+    BBS_MAX_CELLS cells.  Class totals reach 1.5e7, just below 2^24, where
+    FP32 still holds every integer; the fixed-point sums of the sum score
+    reach 2^43 of their 2^48 range."""
+    G, Cn = 255, 65535
+    m, _, _ = D.generate_dataset(7 * G + Cn, G, Cn, 1e-3, 0.2, 0.05, 0.01)
+    mut, known = D.matrix_to_bits(m)
+    return G, Cn, m, mut, known
+
+
+def test_largest_problem_scores(native, orc, largest):
+    G, Cn, m, mut, known = largest
+    rng = np.random.default_rng(65535)
+    parents = [D.random_parent_vector(rng, G) for _ in range(3)]
+    dms = tree_stack(orc, parents)
+    betas = np.array([0.2, 0.05, 0.45], dtype=np.float32)
+    c, _, _ = ctx_for(native, m, 1e-3, 0.2)
+    with c:
+        s, counts, att = c.score_trees(dms, betas, attach=True)
+        logl, da, db, _ = c.sumscore_grad(dms, 1e-3, betas)
+    for t in range(3):
+        _, st, oc, oatt = orc.logscore_tree(1e-3, 0.2, 0.1, dms[t], mut,
+                                            known, float(betas[t]))
+        assert np.float32(s[t]) == np.float32(st)
+        assert (counts[t] == oc).all() and (att[t] == oatt).all()
+        # the four classes partition the known entries
+        assert int(counts[t].sum()) == int(np.unpackbits(
+            known.view(np.uint8)).sum())
+        f64 = orc.logscore_tree_f64(1e-3, float(betas[t]), dms[t], mut, known,
+                                    0.2, 0.1, True)
+        assert abs(s[t] - f64) <= SCORE_RTOL * abs(f64)
+        f, ga, gb, _ = orc.sumscore_grad_f64(1e-3, float(betas[t]), dms[t],
+                                             mut, known)
+        assert abs(logl[t] - f) <= SCORE_RTOL * abs(f)
+        assert abs(da[t] - ga) <= GRAD_RTOL * abs(ga)
+        assert abs(db[t] - gb) <= GRAD_RTOL * abs(gb)
+
+
+def test_largest_problem_replays(native, orc, largest):
+    G, Cn, m, _, _ = largest
+    mp = orc.move_probs(0.0, 0.55, 0.4, 0.05)
+    raws = orc.sample_moves(mp, G + 1, 77, 0, 20)[None]
+    start = [D.random_parent_vector(np.random.default_rng(5), G)]
+    _replay_check(native, orc, m, 1e-3, 0.2, start, raws)
+
+
 def test_philox_stream_matches_oracle(native, orc):
     G, Cn = 40, 50
     m, _, _ = D.generate_dataset(1, G, Cn, 1e-3, 0.2, 0.1, 0.0)
