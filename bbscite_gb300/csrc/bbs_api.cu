@@ -239,6 +239,7 @@ struct bbs_ctx {
   // scratch_cap bytes each; grows, never shrinks
   uint8_t *d_scratch = nullptr, *h_scratch = nullptr;
   size_t scratch_cap = 0;
+  uint64_t fingerprint = 0;  // of the dataset and parameters (checkpoints)
 };
 
 namespace {
@@ -452,6 +453,90 @@ class ScratchPlan {
   size_t bytes_ = 0;
   size_t off_ = 0;
 };
+
+// FNV-1a, 64 bit.
+uint64_t fnv1a(uint64_t h, const void *p, size_t n) {
+  const uint8_t *b = static_cast<const uint8_t *>(p);
+  for (size_t i = 0; i < n; i++) {
+    h ^= b[i];
+    h *= 0x100000001B3ull;
+  }
+  return h;
+}
+
+template <typename T>
+uint64_t fnv1a_of(uint64_t h, const T &v) {
+  return fnv1a(h, &v, sizeof(T));
+}
+
+// The dataset as the kernels see it and every parameter field (not the
+// struct's padding).
+uint64_t context_fingerprint(const bbs_params &p, uint32_t n_cells,
+                             uint32_t n_genes, const std::vector<uint64_t> &K,
+                             const std::vector<uint64_t> &M) {
+  uint64_t h = 0xCBF29CE484222325ull;
+  h = fnv1a_of(h, n_cells);
+  h = fnv1a_of(h, n_genes);
+  h = fnv1a(h, K.data(), sizeof(uint64_t) * K.size());
+  h = fnv1a(h, M.data(), sizeof(uint64_t) * M.size());
+  for (const float f : {p.alpha_mean, p.beta_mean, p.beta_sd, p.prob_beta_change,
+                        p.prob_prune_n_reattach, p.prob_swap_nodes,
+                        p.prob_swap_subtrees, p.beta_jump_scaling_chi, p.gamma,
+                        p.error_step})
+    h = fnv1a_of(h, f);
+  for (const uint32_t u : {p.treelist_size, p.score_mode, p.error_move})
+    h = fnv1a_of(h, u);
+  return fnv1a_of(h, p.seed);
+}
+
+// True when dm (n rows of W words) is the descendant matrix of a tree
+// rooted at n-1: its parent vector is valid and gives back the same rows.
+bool valid_tree_rows(const uint64_t *dm, uint32_t n, std::vector<uint32_t> &pv,
+                     std::vector<uint64_t> &tmp) {
+  const uint32_t W = words64(n);
+  pv.resize(n);
+  tmp.resize((size_t)n * W);
+  matrix_to_parent(dm, n, pv.data());
+  if (check_parent_vector(pv.data(), n) != BBS_OK) return false;
+  parent_to_matrix(pv.data(), n, nullptr, tmp.data());
+  return std::memcmp(tmp.data(), dm, sizeof(uint64_t) * tmp.size()) == 0;
+}
+
+// Layout of a chain checkpoint: this header, then the current rows
+// (n_chains x n_nodes x W words), the best rows (n_chains x treelist x
+// n_nodes x W), the chain states (n_chains x 128 bytes) and, with
+// treelist > 1, the tree hashes (n_chains x treelist) and betas of the
+// co-optimal lists, padded to 8 bytes.
+struct CheckpointHeader {
+  char magic[8];
+  uint32_t version, header_bytes;
+  uint64_t fingerprint;
+  uint32_t n_nodes, n_cells, words, n_chains;
+  uint32_t treelist, state_bytes;
+  uint64_t total_bytes;
+  uint64_t reserved[3];
+};
+static_assert(sizeof(CheckpointHeader) == 80, "checkpoint header layout");
+constexpr char kCheckpointMagic[8] = {'B', 'B', 'S', 'C', 'H', 'K', 'P', 'T'};
+constexpr uint32_t kCheckpointVersion = 1;
+
+struct CheckpointSizes {
+  size_t rows, best, states, hashes, betas, total;
+};
+
+CheckpointSizes checkpoint_sizes(uint32_t n_nodes, uint32_t n_chains,
+                                 uint32_t K) {
+  CheckpointSizes z{};
+  const size_t tw = (size_t)n_nodes * words64(n_nodes);
+  z.rows = sizeof(uint64_t) * tw * n_chains;
+  z.best = z.rows * K;
+  z.states = sizeof(ChainState) * n_chains;
+  z.hashes = K > 1 ? sizeof(uint64_t) * n_chains * K : 0;
+  z.betas = K > 1 ? (sizeof(float) * n_chains * K + 7) / 8 * 8 : 0;
+  z.total = sizeof(CheckpointHeader) + z.rows + z.best + z.states + z.hashes +
+            z.betas;
+  return z;
+}
 
 }  // namespace
 
@@ -682,6 +767,7 @@ int bbs_create(bbs_ctx **out, const uint64_t *is_mutated,
     c->ds = h.ds;
     c->md = h.md;
     std::memcpy(c->terms, h.terms, sizeof(h.terms));
+    c->fingerprint = context_fingerprint(*params, n_cells, n_genes, h.K, h.M);
     c->q = pick_q((int)n_cells);
     *out = c;
     return BBS_OK;
@@ -1167,6 +1253,131 @@ int bbs_get_treelist(bbs_ctx *c, uint32_t max_trees, uint64_t *dm,
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_get_treelist");
+  }
+}
+
+int bbs_save_chains(bbs_ctx *c, void *buf, size_t *size) {
+  try {
+    if (!c || !size) return fail(BBS_ERR_INPUT, "NULL argument");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    if (c->n_chains == 0) return fail(BBS_ERR_STATE, "no chains");
+    const CheckpointSizes z = checkpoint_sizes(c->n_nodes, c->n_chains, c->K);
+    if (!buf) {
+      *size = z.total;
+      return BBS_OK;
+    }
+    if (*size < z.total) {
+      const size_t have = *size;
+      *size = z.total;
+      return fail(BBS_ERR_SIZE, "checkpoint needs %zu bytes, buffer has %zu",
+                  z.total, have);
+    }
+    CheckpointHeader hd{};
+    std::memcpy(hd.magic, kCheckpointMagic, sizeof(hd.magic));
+    hd.version = kCheckpointVersion;
+    hd.header_bytes = sizeof(CheckpointHeader);
+    hd.fingerprint = c->fingerprint;
+    hd.n_nodes = c->n_nodes;
+    hd.n_cells = c->n_cells;
+    hd.words = c->W64;
+    hd.n_chains = c->n_chains;
+    hd.treelist = c->K;
+    hd.state_bytes = sizeof(ChainState);
+    hd.total_bytes = z.total;
+    uint8_t *p = static_cast<uint8_t *>(buf);
+    std::memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    BBS_CUDA(cudaMemcpy(p, c->d_rows, z.rows, cudaMemcpyDeviceToHost), "checkpoint copy");
+    p += z.rows;
+    BBS_CUDA(cudaMemcpy(p, c->d_best, z.best, cudaMemcpyDeviceToHost), "checkpoint copy");
+    p += z.best;
+    BBS_CUDA(cudaMemcpy(p, c->d_states, z.states, cudaMemcpyDeviceToHost), "checkpoint copy");
+    p += z.states;
+    if (c->K > 1) {
+      BBS_CUDA(cudaMemcpy(p, c->d_lhash, z.hashes, cudaMemcpyDeviceToHost), "checkpoint copy");
+      p += z.hashes;
+      std::memset(p, 0, z.betas);
+      BBS_CUDA(cudaMemcpy(p, c->d_lbeta, sizeof(float) * c->n_chains * c->K,
+                          cudaMemcpyDeviceToHost), "checkpoint copy");
+    }
+    *size = z.total;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_save_chains");
+  }
+}
+
+int bbs_load_chains(bbs_ctx *c, const void *buf, size_t size) {
+  try {
+    if (!c || !buf) return fail(BBS_ERR_INPUT, "NULL argument");
+    if (c->running) return fail(BBS_ERR_STATE, "a run is in progress");
+    CheckpointHeader hd;
+    if (size < sizeof(hd)) return fail(BBS_ERR_INPUT, "checkpoint too short");
+    std::memcpy(&hd, buf, sizeof(hd));
+    if (std::memcmp(hd.magic, kCheckpointMagic, sizeof(hd.magic)) != 0)
+      return fail(BBS_ERR_INPUT, "not a chain checkpoint");
+    if (hd.version != kCheckpointVersion || hd.header_bytes != sizeof(hd) ||
+        hd.state_bytes != sizeof(ChainState))
+      return fail(BBS_ERR_INPUT, "checkpoint version %u is not supported",
+                  hd.version);
+    if (hd.fingerprint != c->fingerprint || hd.n_nodes != c->n_nodes ||
+        hd.n_cells != c->n_cells || hd.words != c->W64 ||
+        hd.treelist != (uint32_t)c->md.treelist)
+      return fail(BBS_ERR_INPUT,
+                  "the checkpoint was made with another dataset or other "
+                  "parameters");
+    if (hd.n_chains < 1) return fail(BBS_ERR_INPUT, "checkpoint has no chains");
+    const uint32_t n = c->n_nodes, K = hd.treelist;
+    const CheckpointSizes z = checkpoint_sizes(n, hd.n_chains, K);
+    if (hd.total_bytes != z.total || size < z.total)
+      return fail(BBS_ERR_INPUT, "checkpoint size %zu, expected %zu", size,
+                  z.total);
+    const uint8_t *p = static_cast<const uint8_t *>(buf) + sizeof(hd);
+    const uint64_t *rows = reinterpret_cast<const uint64_t *>(p);
+    const uint64_t *best = reinterpret_cast<const uint64_t *>(p + z.rows);
+    std::vector<ChainState> st(hd.n_chains);
+    std::memcpy(st.data(), p + z.rows + z.best, z.states);
+    // every tree the kernels will read must be a tree: moves walk its rows
+    const size_t tw = (size_t)n * c->W64;
+    std::vector<uint32_t> pv;
+    std::vector<uint64_t> tmp;
+    for (uint32_t i = 0; i < hd.n_chains; i++) {
+      if (!valid_tree_rows(rows + i * tw, n, pv, tmp))
+        return fail(BBS_ERR_INPUT, "checkpoint chain %u holds no valid tree", i);
+      if (st[i].list_count > K || st[i].has_best > 1)
+        return fail(BBS_ERR_INPUT, "checkpoint chain %u has a bad state", i);
+      const uint32_t listed = st[i].has_best ? (K > 1 ? st[i].list_count : 1u) : 0u;
+      for (uint32_t j = 0; j < listed; j++)
+        if (!valid_tree_rows(best + ((size_t)i * K + j) * tw, n, pv, tmp))
+          return fail(BBS_ERR_INPUT, "checkpoint chain %u holds no valid best tree", i);
+    }
+    free_chains(c);
+    c->K = K;
+    cudaError_t e = cudaMalloc(&c->d_rows, z.rows);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_best, z.best);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_states, z.states);
+    if (e == cudaSuccess && K > 1) e = cudaMalloc(&c->d_lhash, z.hashes);
+    if (e == cudaSuccess && K > 1)
+      e = cudaMalloc(&c->d_lbeta, sizeof(float) * hd.n_chains * K);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_rows, rows, z.rows, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c->d_best, best, z.best, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(c->d_states, st.data(), z.states, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && K > 1)
+      e = cudaMemcpy(c->d_lhash, p + z.rows + z.best + z.states, z.hashes,
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && K > 1)
+      e = cudaMemcpy(c->d_lbeta, p + z.rows + z.best + z.states + z.hashes,
+                     sizeof(float) * hd.n_chains * K, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      free_chains(c);
+      return cuda_fail((int)e, "bbs_load_chains");
+    }
+    c->n_chains = hd.n_chains;
+    default_launch(c);
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_load_chains");
   }
 }
 

@@ -100,6 +100,8 @@ def lib():
         "bbs_get_chains": (C.c_int, [v, v, v, v, v, v, v]),
         "bbs_get_best_alpha": (C.c_int, [v, v]),
         "bbs_get_treelist": (C.c_int, [v, u32, v, v, v, v]),
+        "bbs_save_chains": (C.c_int, [v, v, v]),
+        "bbs_load_chains": (C.c_int, [v, v, C.c_size_t]),
         "bbs_batch_create": (C.c_int, [v, u32, v, v, v, v, v]),
         "bbs_batch_destroy": (None, [v]),
         "bbs_batch_init_chains": (C.c_int, [v, u32]),
@@ -338,6 +340,22 @@ class Context:
         a = C.c_float()
         check(lib().bbs_get_best_alpha(self._h, C.byref(a)))
         return a.value
+
+    def save_chains(self) -> bytes:
+        """Every chain's state as one checkpoint image (bbs_save_chains)."""
+        size = C.c_size_t()
+        check(lib().bbs_save_chains(self._h, None, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        check(lib().bbs_save_chains(self._h, buf, C.byref(size)))
+        return buf.raw[:size.value]
+
+    def load_chains(self, image: bytes) -> None:
+        """Replaces the chains with those of a checkpoint image made with
+        the same dataset and parameters (bbs_load_chains)."""
+        check(lib().bbs_load_chains(self._h, image, len(image)))
+        n = C.c_uint32()
+        check(lib().bbs_get_sizes(self._h, None, None, C.byref(n)))
+        self.n_chains = n.value
 
     # -- batch primitives --
     def score_trees(self, dm, betas, attach: bool = False):

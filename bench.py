@@ -550,10 +550,11 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
     plain = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5)
     out = {"n_genes": G, "n_cells": Cn, "chains": chains, "steps": steps,
            "warm_up_steps": warm}
+    # launch shapes are tuned on the warmed-up chains, the regime timed
     with N.Batch([(mut, known, Cn, G)], adj) as bt:
         bt.init_chains(chains)
-        bt.autotune(max(8, steps // 10))
         bt.run(warm)
+        bt.autotune(max(8, steps // 4))
         flush.zero_()
         torch.cuda.synchronize()
         bt.run(steps)
@@ -562,8 +563,8 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
         out["batched_launch"] = list(bt.launch())
     with N.Context(mut, known, Cn, G, plain) as c:
         c.init_chains(chains)
-        c.autotune(max(8, steps // 10))
         c.run(warm)
+        c.autotune(max(8, steps // 4))
         flush.zero_()
         torch.cuda.synchronize()
         c.run(steps)

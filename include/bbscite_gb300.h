@@ -246,6 +246,22 @@ BBS_API int bbs_get_best_alpha(bbs_ctx *ctx, float *alpha);
 BBS_API int bbs_get_chains(bbs_ctx *ctx, uint64_t *dm, float *alpha, float *beta,
                    float *score, uint64_t *counts, uint32_t *err_stats);
 
+/* Chain checkpoints (no counterpart in the reference, whose chain state
+ * lives only inside the FPGA pipeline, src/Application.hpp:490-495).
+ * bbs_save_chains writes every chain's state -- current and best trees,
+ * the co-optimal lists, rates, scores, error-move statistics and the
+ * position in its Philox stream -- into buf as one byte image of *size
+ * bytes; with buf == NULL it only sets *size.  A buffer that is too small
+ * gives BBS_ERR_SIZE with the size needed in *size.  bbs_load_chains
+ * restores such an image into a context created with the same dataset and
+ * parameters (in this process or another), replacing its chains; the
+ * chains then continue exactly as if they had never stopped.  An image of
+ * another dataset or other parameters, a damaged image or one holding
+ * something other than trees gives BBS_ERR_INPUT and leaves the context's
+ * chains as they were.  The launch shape returns to its default. */
+BBS_API int bbs_save_chains(bbs_ctx *ctx, void *buf, size_t *size);
+BBS_API int bbs_load_chains(bbs_ctx *ctx, const void *buf, size_t size);
+
 /* TreeScorer::logscore_tree for a batch, src/TreeScorer.hpp:131-210:
  * dm = n_trees x n_nodes x W ancestor rows, betas (n_trees).  Outputs:
  * scores (class-total form: ((l00*N00 + l01*N01) + l10*N10) + l11*N11 plus

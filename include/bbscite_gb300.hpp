@@ -589,6 +589,21 @@ class Application {
                        betas[i]);
     return out;
   }
+  /* Chain checkpoints (bbs_save_chains / bbs_load_chains): the image of
+   * every chain's state, and its restoration into an Application made with
+   * the same data and parameters, after which run_simulation continues the
+   * chains exactly. */
+  std::vector<uint8_t> save_chains() {
+    size_t size = 0;
+    check(bbs_save_chains(ctx.get(), nullptr, &size));
+    std::vector<uint8_t> image(size);
+    check(bbs_save_chains(ctx.get(), image.data(), &size));
+    return image;
+  }
+  void load_chains(std::vector<uint8_t> const &image) {
+    check(bbs_load_chains(ctx.get(), image.data(), image.size()));
+    fetched = false;
+  }
   bbs_ctx *handle() { return ctx.get(); }
 
  private:

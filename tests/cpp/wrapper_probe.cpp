@@ -9,10 +9,14 @@
 //   scorer <alpha> <beta> <sd> <n_cells> <n_genes> <mut words...> <known words...>
 //   score                       logscore_tree of the current tree (device)
 //   prior <beta>                logscore_beta (context on the device)
+//   resume <n_cells> <n_genes> <steps1> <steps2> <mut words...> <known words...> <argv...>
+//                               Application run for steps1 + steps2 vs run
+//                               for steps1, saved, restored and run for steps2
 #include <iomanip>
 #include <iostream>
 #include <memory>
 #include <sstream>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -145,6 +149,40 @@ void run(const std::string &line, State &st) {
     float b;
     in >> b;
     std::cout << std::setprecision(9) << st.scorer->logscore_beta(b) << "\n";
+  } else if (cmd == "resume") {
+    uint32_t nc, ng, s1, s2;
+    in >> nc >> ng >> s1 >> s2;
+    const size_t words = (size_t)nc * bbs_words(ng + 1);
+    std::vector<uint64_t> mut(words), known(words);
+    for (auto &w : mut) in >> w;
+    for (auto &w : known) in >> w;
+    std::vector<std::string> rest;
+    std::string t;
+    while (in >> t) rest.push_back(t);
+    auto params_for = [&](uint32_t steps) {
+      std::vector<std::string> tok{"bbscite"};
+      tok.insert(tok.end(), rest.begin(), rest.end());
+      tok.push_back("-l");
+      tok.push_back(std::to_string(steps));
+      std::vector<char *> argv;
+      for (auto &s : tok) argv.push_back(s.data());
+      Parameters p;
+      if (!p.load_and_verify_args((int)argv.size(), argv.data()))
+        throw std::runtime_error("bad arguments");
+      return p;
+    };
+    Application whole(mut, known, params_for(s1 + s2), nc, ng);
+    whole.run_simulation();
+    Application first(mut, known, params_for(s1), nc, ng);
+    first.run_simulation();
+    const std::vector<uint8_t> image = first.save_chains();
+    Application second(mut, known, params_for(s2), nc, ng);
+    second.load_chains(image);
+    second.run_simulation();
+    std::cout << std::setprecision(9) << "whole " << whole.get_best_score()
+              << " resumed " << second.get_best_score() << " same_tree "
+              << (whole.get_best_dm() == second.get_best_dm()) << " bytes "
+              << image.size() << "\n";
   } else {
     std::cout << "unknown command\n";
   }

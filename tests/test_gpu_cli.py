@@ -122,6 +122,23 @@ def test_cpp_tree_scorer_kat(probe, kat, orc):
     assert score == pytest.approx(want, rel=k["catch_approx_rel"])
 
 
+def test_cpp_application_checkpoint(probe):
+    """Application::save_chains / load_chains: a run of 300 + 200 steps
+    split by a checkpoint into a second Application ends where one run of
+    500 steps does."""
+    G, Cn = 20, 30
+    m, _, _ = D.generate_dataset(11, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    words = " ".join(str(int(w)) for w in list(mut.ravel()) +
+                     list(known.ravel()))
+    out, _ = probe([f"resume {Cn} {G} 300 200 {words} -i in.csv -r 4 "
+                    "-fd 0.001 -ad 0.2 -e 0.1 -seed 9"])
+    f = out[0].split()
+    assert f[0] == "whole" and f[2] == "resumed"
+    assert float(f[1]) == float(f[3])
+    assert f[5] == "1"
+
+
 def test_cli_application_kat(native, orc, kat, tmp_path):
     """The reference's end-to-end test (test/Application.cpp:38-143)
     through the command line: the tree in _ml0 scores like the true tree
