@@ -1742,6 +1742,7 @@ struct bbs_batch {
   cudaGraphExec_t graph = nullptr;
   uint32_t graph_steps = 0;
   float last_ms = 0.0f;
+  uint64_t fingerprint = 0;  // of all datasets and parameters (checkpoints)
 };
 
 namespace {
@@ -1767,6 +1768,60 @@ void batch_free_chains(bbs_batch *b) {
   b->d_chain_off = nullptr;
   b->n_chains = 0;
 }
+
+// The chain layout of a batch with cpd chains per dataset: chain c of
+// dataset d is c = d * cpd + k, and its rows start at chain_off[c]
+// (32-bit words, 32-byte aligned).  Returns the row words of all chains.
+size_t batch_layout(bbs_batch *b, uint32_t cpd) {
+  const uint32_t n_chains = cpd * b->n_datasets;
+  b->chain_ds.resize(n_chains);
+  b->chain_off.resize(n_chains);
+  size_t words = 0;
+  for (uint32_t d = 0; d < b->n_datasets; d++)
+    for (uint32_t k = 0; k < cpd; k++) {
+      const uint32_t c = d * cpd + k;
+      const uint32_t n = b->n_genes[d] + 1;
+      b->chain_ds[c] = d;
+      b->chain_off[c] = words;
+      words += (size_t)n * 2 * words64(n);
+      words = (words + 7) & ~(size_t)7;  // 32-byte aligned rows
+    }
+  b->row_words = words;
+  return words;
+}
+
+// Device arrays of the layout batch_layout made (contents not set).
+cudaError_t batch_alloc_chains(bbs_batch *b) {
+  const size_t n_chains = b->chain_ds.size(), words = b->row_words;
+  cudaError_t e = cudaMalloc(&b->d_rows, sizeof(uint32_t) * words);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_best, sizeof(uint32_t) * words);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_states, sizeof(ChainState) * n_chains);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_ds, sizeof(uint32_t) * n_chains);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_off, sizeof(uint64_t) * n_chains);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_chain_ds, b->chain_ds.data(), sizeof(uint32_t) * n_chains,
+                   cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->d_chain_off, b->chain_off.data(), sizeof(uint64_t) * n_chains,
+                   cudaMemcpyHostToDevice);
+  return e;
+}
+
+// Layout of a batch checkpoint: this header, then the current rows and
+// the best rows (row_words 32-bit words each, in the batch_layout order)
+// and the chain states (128 bytes each).
+struct BatchCheckpointHeader {
+  char magic[8];
+  uint32_t version, header_bytes;
+  uint64_t fingerprint;
+  uint32_t n_datasets, chains_per_dataset;
+  uint32_t state_bytes, reserved0;
+  uint64_t row_words;
+  uint64_t total_bytes;
+  uint64_t reserved[2];
+};
+static_assert(sizeof(BatchCheckpointHeader) == 72, "batch checkpoint header layout");
+constexpr char kBatchCheckpointMagic[8] = {'B', 'B', 'S', 'B', 'A', 'T', 'C', 'H'};
 
 // Launch groups for the current shape: one per row width (exact, or the
 // even width of its row stride with merge), chains costliest first.
@@ -1896,6 +1951,9 @@ int bbs_batch_create(bbs_batch **out, uint32_t n_datasets,
     for (uint32_t d = 0; d < n_datasets; d++) {
       prepare_dataset(&params[d], n_cells[d], n_genes[d], is_mutated[d],
                       is_known[d], h[d]);
+      const uint64_t f = context_fingerprint(params[d], n_cells[d], n_genes[d],
+                                             h[d].K, h[d].M);
+      b->fingerprint = fnv1a_of(d == 0 ? 0xCBF29CE484222325ull : b->fingerprint, f);
       off[d] = words;
       words += 2 * h[d].K.size();  // uint32 words of K, then of M
       words = (words + 7) & ~(size_t)7;
@@ -1968,37 +2026,15 @@ int bbs_batch_init_chains(bbs_batch *b, uint32_t cpd) {
     if (cpd < 1) return fail(BBS_ERR_INPUT, "need at least one chain per dataset");
     batch_free_chains(b);
     const uint32_t n_chains = cpd * b->n_datasets;
-    b->chain_ds.resize(n_chains);
-    b->chain_off.resize(n_chains);
-    size_t words = 0;
-    for (uint32_t d = 0; d < b->n_datasets; d++)
-      for (uint32_t k = 0; k < cpd; k++) {
-        const uint32_t c = d * cpd + k;
-        const uint32_t n = b->n_genes[d] + 1;
-        b->chain_ds[c] = d;
-        b->chain_off[c] = words;
-        words += (size_t)n * 2 * words64(n);
-        words = (words + 7) & ~(size_t)7;  // 32-byte aligned rows
-      }
-    b->row_words = words;
+    const size_t words = batch_layout(b, cpd);
     uint32_t max_nodes = 0;
     for (uint32_t d = 0; d < b->n_datasets; d++)
       max_nodes = std::max(max_nodes, b->n_genes[d] + 1);
-    cudaError_t e = cudaMalloc(&b->d_rows, sizeof(uint32_t) * words);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_best, sizeof(uint32_t) * words);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_states, sizeof(ChainState) * n_chains);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_ds, sizeof(uint32_t) * n_chains);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_chain_off, sizeof(uint64_t) * n_chains);
+    cudaError_t e = batch_alloc_chains(b);
     if (e == cudaSuccess)
       e = cudaMemsetAsync(b->d_rows, 0, sizeof(uint32_t) * words, b->stream);
     if (e == cudaSuccess)
       e = cudaMemsetAsync(b->d_best, 0, sizeof(uint32_t) * words, b->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(b->d_chain_ds, b->chain_ds.data(), sizeof(uint32_t) * n_chains,
-                     cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(b->d_chain_off, b->chain_off.data(), sizeof(uint64_t) * n_chains,
-                     cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
       // every dataset's random initial trees, drawn on the device
       TreeArgs ta{};
@@ -2186,6 +2222,119 @@ int bbs_batch_get_best(bbs_batch *b, uint32_t dataset, uint64_t *dm,
     return BBS_OK;
   } catch (...) {
     return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_get_best");
+  }
+}
+
+int bbs_batch_save_chains(bbs_batch *b, void *buf, size_t *size) {
+  try {
+    if (!b || !size) return fail(BBS_ERR_INPUT, "NULL argument");
+    if (b->n_chains == 0) return fail(BBS_ERR_STATE, "no chains");
+    const size_t rows = sizeof(uint32_t) * b->row_words;
+    const size_t states = sizeof(ChainState) * b->n_chains;
+    const size_t total = sizeof(BatchCheckpointHeader) + 2 * rows + states;
+    if (!buf) {
+      *size = total;
+      return BBS_OK;
+    }
+    if (*size < total) {
+      const size_t have = *size;
+      *size = total;
+      return fail(BBS_ERR_SIZE, "checkpoint needs %zu bytes, buffer has %zu",
+                  total, have);
+    }
+    BatchCheckpointHeader hd{};
+    std::memcpy(hd.magic, kBatchCheckpointMagic, sizeof(hd.magic));
+    hd.version = kCheckpointVersion;
+    hd.header_bytes = sizeof(hd);
+    hd.fingerprint = b->fingerprint;
+    hd.n_datasets = b->n_datasets;
+    hd.chains_per_dataset = b->cpd;
+    hd.state_bytes = sizeof(ChainState);
+    hd.row_words = b->row_words;
+    hd.total_bytes = total;
+    uint8_t *p = static_cast<uint8_t *>(buf);
+    std::memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    BBS_CUDA(cudaStreamSynchronize(b->stream), "batch stream");
+    BBS_CUDA(cudaMemcpy(p, b->d_rows, rows, cudaMemcpyDeviceToHost), "checkpoint copy");
+    BBS_CUDA(cudaMemcpy(p + rows, b->d_best, rows, cudaMemcpyDeviceToHost),
+             "checkpoint copy");
+    BBS_CUDA(cudaMemcpy(p + 2 * rows, b->d_states, states, cudaMemcpyDeviceToHost),
+             "checkpoint copy");
+    *size = total;
+    return BBS_OK;
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_save_chains");
+  }
+}
+
+int bbs_batch_load_chains(bbs_batch *b, const void *buf, size_t size) {
+  try {
+    if (!b || !buf) return fail(BBS_ERR_INPUT, "NULL argument");
+    BatchCheckpointHeader hd;
+    if (size < sizeof(hd)) return fail(BBS_ERR_INPUT, "checkpoint too short");
+    std::memcpy(&hd, buf, sizeof(hd));
+    if (std::memcmp(hd.magic, kBatchCheckpointMagic, sizeof(hd.magic)) != 0)
+      return fail(BBS_ERR_INPUT, "not a batch checkpoint");
+    if (hd.version != kCheckpointVersion || hd.header_bytes != sizeof(hd) ||
+        hd.state_bytes != sizeof(ChainState))
+      return fail(BBS_ERR_INPUT, "checkpoint version %u is not supported",
+                  hd.version);
+    if (hd.fingerprint != b->fingerprint || hd.n_datasets != b->n_datasets)
+      return fail(BBS_ERR_INPUT,
+                  "the checkpoint was made with other datasets or other "
+                  "parameters");
+    const uint32_t cpd = hd.chains_per_dataset;
+    if (cpd < 1 || (uint64_t)cpd * b->n_datasets * sizeof(ChainState) > size)
+      return fail(BBS_ERR_INPUT, "checkpoint of %u chains per dataset does not "
+                  "fit in %zu bytes", cpd, size);
+    // the layout of cpd chains per dataset, on a scratch copy of the batch's
+    // tables so that a refused image leaves the batch as it was
+    bbs_batch probe;
+    probe.n_datasets = b->n_datasets;
+    probe.n_genes = b->n_genes;
+    const size_t words = batch_layout(&probe, cpd);
+    const uint32_t n_chains = cpd * b->n_datasets;
+    const size_t rows = sizeof(uint32_t) * words;
+    const size_t states = sizeof(ChainState) * n_chains;
+    const size_t total = sizeof(hd) + 2 * rows + states;
+    if (hd.row_words != words || hd.total_bytes != total || size < total)
+      return fail(BBS_ERR_INPUT, "checkpoint size %zu, expected %zu", size, total);
+    const uint8_t *p = static_cast<const uint8_t *>(buf) + sizeof(hd);
+    std::vector<ChainState> st(n_chains);
+    std::memcpy(st.data(), p + 2 * rows, states);
+    std::vector<uint32_t> pv;
+    std::vector<uint64_t> tmp;
+    for (uint32_t c = 0; c < n_chains; c++) {
+      const uint32_t n = b->n_genes[probe.chain_ds[c]] + 1;
+      const uint64_t *cur =
+          reinterpret_cast<const uint64_t *>(p) + probe.chain_off[c] / 2;
+      const uint64_t *bst =
+          reinterpret_cast<const uint64_t *>(p + rows) + probe.chain_off[c] / 2;
+      if (!valid_tree_rows(cur, n, pv, tmp))
+        return fail(BBS_ERR_INPUT, "checkpoint chain %u holds no valid tree", c);
+      if (st[c].has_best > 1 || st[c].list_count > 1)
+        return fail(BBS_ERR_INPUT, "checkpoint chain %u has a bad state", c);
+      if (st[c].has_best && !valid_tree_rows(bst, n, pv, tmp))
+        return fail(BBS_ERR_INPUT, "checkpoint chain %u holds no valid best tree", c);
+    }
+    BBS_CUDA(cudaStreamSynchronize(b->stream), "batch stream");
+    batch_free_chains(b);
+    batch_layout(b, cpd);
+    cudaError_t e = batch_alloc_chains(b);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_rows, p, rows, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_best, p + rows, rows, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->d_states, st.data(), states, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      batch_free_chains(b);
+      return cuda_fail((int)e, "bbs_batch_load_chains");
+    }
+    b->cpd = cpd;
+    b->n_chains = n_chains;
+    return batch_build_groups(b);
+  } catch (...) {
+    return fail(BBS_ERR_ALLOC, "allocation failed in bbs_batch_load_chains");
   }
 }
 

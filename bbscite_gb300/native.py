@@ -111,6 +111,8 @@ def lib():
         "bbs_batch_get_launch": (C.c_int, [v, v, v, v]),
         "bbs_batch_autotune": (C.c_int, [v, u32, v]),
         "bbs_batch_get_best": (C.c_int, [v, u32, v, v, v, v, v]),
+        "bbs_batch_save_chains": (C.c_int, [v, v, v]),
+        "bbs_batch_load_chains": (C.c_int, [v, v, C.c_size_t]),
         "bbs_score_trees": (C.c_int, [v, v, v, u32, v, v, v]),
         "bbs_apply_moves": (C.c_int, [v, v, v, u32, v, v, v, v, v]),
         "bbs_sumscore_grad": (C.c_int, [v, v, v, v, u32, v, v, v, v]),
@@ -473,6 +475,19 @@ class Batch:
         ms = C.c_float()
         check(lib().bbs_batch_autotune(self._h, probe_steps, C.byref(ms)))
         return ms.value
+
+    def save_chains(self) -> bytes:
+        """Every chain of every dataset as one checkpoint image."""
+        size = C.c_size_t()
+        check(lib().bbs_batch_save_chains(self._h, None, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        check(lib().bbs_batch_save_chains(self._h, buf, C.byref(size)))
+        return buf.raw[:size.value]
+
+    def load_chains(self, image: bytes) -> None:
+        """Replaces the chains with those of a checkpoint image made with
+        the same datasets and parameters."""
+        check(lib().bbs_batch_load_chains(self._h, image, len(image)))
 
     def best(self, dataset: int) -> dict:
         n = int(self.n_genes[dataset]) + 1

@@ -328,6 +328,11 @@ BBS_API int bbs_batch_autotune(bbs_batch *batch, uint32_t probe_steps,
 BBS_API int bbs_batch_get_best(bbs_batch *batch, uint32_t dataset, uint64_t *dm,
                                uint32_t *parent, float *alpha, float *beta,
                                float *score);
+/* Checkpoints of a batch, as bbs_save_chains / bbs_load_chains: every
+ * chain of every dataset, restored into a batch created with the same
+ * datasets and parameters. */
+BBS_API int bbs_batch_save_chains(bbs_batch *batch, void *buf, size_t *size);
+BBS_API int bbs_batch_load_chains(bbs_batch *batch, const void *buf, size_t size);
 
 /* Sum-over-attachments score and its adjoint (no counterpart in the
  * reference; SCITE's "-s" score, see docs/thesis/chapters/conclusion/

@@ -144,3 +144,51 @@ def test_save_reports_the_size_it_needs(native):
         assert L.bbs_save_chains(c._h, buf, C.byref(small)) == \
             native.BBS_ERR_SIZE
         assert small.value == size.value
+
+
+def test_batch_resume_from_checkpoint_equals_one_run(native):
+    """A batch of three datasets (three row widths), sum score with
+    Langevin error moves: 200 steps, checkpoint, a new batch, 300 steps
+    end where 500 steps in one batch do."""
+    shapes = [(20, 30), (70, 100), (150, 64)]
+    data = []
+    for i, (g, cn) in enumerate(shapes):
+        m, _, _ = D.generate_dataset(40 + i, g, cn, 1e-3, 0.2, 0.1, 0.02)
+        mut, known = D.matrix_to_bits(m)
+        data.append((mut, known, cn, g))
+    p = native.default_params(alpha_mean=1e-2, beta_mean=0.3, seed=13,
+                              prob_beta_change=0.1,
+                              score_mode=native.SCORE_SUM,
+                              error_move=native.ERROR_LANGEVIN)
+
+    def bests(bt):
+        return [bt.best(d) for d in range(len(shapes))]
+
+    with native.Batch(data, p) as bt:
+        bt.init_chains(5)
+        bt.run(500)
+        whole = bests(bt)
+    with native.Batch(data, p) as bt:
+        bt.init_chains(5)
+        bt.run(200)
+        image = bt.save_chains()
+    with native.Batch(data, p) as bt:
+        bt.init_chains(1)
+        bt.load_chains(image)
+        bt.run(300)
+        got = bests(bt)
+    for w, g in zip(whole, got):
+        assert (w["dm"] == g["dm"]).all()
+        assert (w["alpha"], w["beta"], w["score"]) == \
+            (g["alpha"], g["beta"], g["score"])
+    # other datasets refuse the image and keep their chains
+    with native.Batch(data[:2] + [data[0]], p) as bt:
+        bt.init_chains(2)
+        bt.run(10)
+        before = bests(bt)
+        with pytest.raises(native.BbsError) as e:
+            bt.load_chains(image)
+        assert e.value.code == native.BBS_ERR_INPUT
+        after = bests(bt)
+        for w, g in zip(before, after):
+            assert (w["dm"] == g["dm"]).all() and w["score"] == g["score"]
