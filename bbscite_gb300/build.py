@@ -2,9 +2,13 @@
 
     python -m bbscite_gb300.build        # or __graft_entry__.build()
 
+    python -m bbscite_gb300.build --checked   # the build with device checks
+
 Outputs (git-ignored):
   bbscite_gb300/libbbscite_gb300.so   kernels + C ABI (sm_103a)
   bbscite_gb300/bin/bbscite           SCITE-compatible command line
+  bbscite_gb300/libbbscite_gb300_checked.so   the same with BBS_CHECKED:
+      device-side index checks that report BBS_ERR_DEVICE_CHECK
 Translation units are compiled in parallel; nothing is rebuilt when the
 object is newer than every source it depends on.
 """
@@ -23,6 +27,8 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libbbscite_gb300.so")
+BUILD_CHECKED = os.path.join(PKG, "_build_checked")
+LIB_CHECKED = os.path.join(PKG, "libbbscite_gb300_checked.so")
 CLI = os.path.join(PKG, "bin", "bbscite")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -66,13 +72,16 @@ def _deps() -> float:
     return max(os.path.getmtime(f) for f in files)
 
 
-def _compile(unit: str, newest: float, verbose: bool) -> str:
+def _compile(unit: str, newest: float, verbose: bool,
+             checked: bool = False) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    obj = os.path.join(BUILD_CHECKED if checked else BUILD,
+                       unit.replace(".cu", ".o"))
     if (os.path.exists(obj) and os.path.getmtime(obj) >= newest
             and elf_matches_host(obj)):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(["-DBBS_CHECKED"] if checked else []),
+           "-c", src, "-o", obj]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -81,6 +90,24 @@ def _compile(unit: str, newest: float, verbose: bool) -> str:
     if verbose:
         sys.stderr.write(r.stderr)
     return obj
+
+
+def build_checked(verbose: bool = False, jobs: int | None = None) -> str:
+    """The library with device checks (BBS_CHECKED), for tests and
+    debugging; the CLI is not rebuilt."""
+    os.makedirs(BUILD_CHECKED, exist_ok=True)
+    newest = _deps()
+    units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
+    jobs = jobs or min(len(units), os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        objs = list(ex.map(lambda u: _compile(u, newest, verbose, True), units))
+    if not elf_matches_host(LIB_CHECKED) or os.path.getmtime(LIB_CHECKED) < max(
+            os.path.getmtime(o) for o in objs):
+        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", LIB_CHECKED, *objs,
+                            "-lcudart"], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr}")
+    return LIB_CHECKED
 
 
 def build(verbose: bool = False, jobs: int | None = None) -> str:
@@ -112,4 +139,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    if "--checked" in sys.argv:
+        print(build_checked(verbose="-v" in sys.argv))
+    else:
+        print(build(verbose="-v" in sys.argv))

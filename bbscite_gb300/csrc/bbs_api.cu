@@ -38,6 +38,16 @@ int cuda_fail(int err, const char *what) {
               cudaGetErrorString((cudaError_t)err));
 }
 
+// A run's status words: a failed device check (bit 1, with its code, value
+// and limit; BBS_CHECKED builds) or a cancelled run (bit 0).
+int status_result(const int (&st)[kStatusWords]) {
+  if (st[0] & 2)
+    return fail(BBS_ERR_DEVICE_CHECK, "device check %d failed: %u is not below %u",
+                st[1], (unsigned)st[2], (unsigned)st[3]);
+  if (st[0] & 1) return fail(BBS_ERR_TIMEOUT, "the run was cancelled");
+  return BBS_OK;
+}
+
 #define BBS_CUDA(call, what)                                   \
   do {                                                         \
     cudaError_t e_ = (call);                                   \
@@ -743,7 +753,7 @@ int bbs_create(bbs_ctx **out, const uint64_t *is_mutated,
     if (e == cudaSuccess) e = cudaMalloc(&c->d_M, bytes);
     if (e == cudaSuccess) e = cudaMemcpy(c->d_K, h.K.data(), bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(c->d_M, h.M.data(), bytes, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int) * kStatusWords);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
     if (e == cudaSuccess) e = cudaHostAlloc(&c->h_cancel, sizeof(int), cudaHostAllocMapped);
@@ -930,7 +940,8 @@ int start_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *d_moves,
   a.status = c->d_status;
   a.wpc = c->wpc;
   *c->h_cancel = 0;
-  BBS_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream), "cudaMemset");
+  BBS_CUDA(cudaMemsetAsync(c->d_status, 0, sizeof(int) * kStatusWords, c->stream),
+           "cudaMemset");
   BBS_CUDA(cudaEventRecord(c->ev0, c->stream), "cudaEventRecord");
   const int e = launch_mcmc(a, c->q, c->cpb, c->n_sms, c->stream);
   if (e != 0) return cuda_fail(e, "chain kernel launch");
@@ -944,11 +955,10 @@ int finish_run(bbs_ctx *c) {
   if (e != cudaSuccess) return cuda_fail((int)e, "chain kernel");
   e = cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
   if (e != cudaSuccess) return cuda_fail((int)e, "event timing");
-  int status = 0;
-  e = cudaMemcpy(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  int status[kStatusWords] = {};
+  e = cudaMemcpy(status, c->d_status, sizeof(status), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail((int)e, "status read");
-  if (status & 1) return fail(BBS_ERR_TIMEOUT, "the run was cancelled");
-  return BBS_OK;
+  return status_result(status);
 }
 
 }  // namespace
@@ -1600,6 +1610,24 @@ int bbs_sumscore_grad(bbs_ctx *c, const uint64_t *dm, const float *alphas,
   }
 }
 
+int bbs_device_check_selftest(int *enabled, uint32_t *code, uint32_t *value,
+                              uint32_t *limit) {
+  if (!enabled || !code || !value || !limit)
+    return fail(BBS_ERR_INPUT, "NULL argument");
+  int *d = nullptr;
+  BBS_CUDA(cudaMalloc(&d, sizeof(int) * kStatusWords), "cudaMalloc");
+  int st[kStatusWords] = {};
+  cudaError_t e = cudaMemset(d, 0, sizeof(st));
+  if (e == cudaSuccess) e = (cudaError_t)run_check_selftest(d, enabled);
+  if (e == cudaSuccess) e = cudaMemcpy(st, d, sizeof(st), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail((int)e, "device check self-test");
+  *code = (st[0] & 2) ? (uint32_t)st[1] : 0u;
+  *value = (uint32_t)st[2];
+  *limit = (uint32_t)st[3];
+  return BBS_OK;
+}
+
 int bbs_popc_peak(double *popc_per_s, double *sm_clock_hz) {
   if (!popc_per_s || !sm_clock_hz) return fail(BBS_ERR_INPUT, "NULL argument");
   const int e = run_popc_bench(popc_per_s, sm_clock_hz);
@@ -1870,7 +1898,8 @@ int batch_build_groups(bbs_batch *b) {
 int batch_issue(bbs_batch *b, uint32_t n_steps) {
   BBS_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * kMaxW32,
                            b->stream), "memset");
-  BBS_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(int), b->stream), "memset");
+  BBS_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(int) * kStatusWords, b->stream),
+           "memset");
   BBS_CUDA(cudaEventRecord(b->fork, b->stream), "event");
   for (size_t g = 0; g < b->groups.size(); g++) {
     const auto &grp = b->groups[g];
@@ -1882,6 +1911,8 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.chain_off = b->d_chain_off;
     a.units = grp.d_units;
     a.n_units = (int)grp.units.size();
+    a.n_chains = (int)b->n_chains;
+    a.n_datasets = (int)b->n_datasets;
     a.n_steps = (int)n_steps;
     a.chains_per_dataset = (int)b->cpd;
     a.rows = b->d_rows;
@@ -1988,7 +2019,7 @@ int bbs_batch_create(bbs_batch **out, uint32_t n_datasets,
       e = cudaMemcpy(b->d_terms, b->terms.data(), sizeof(float) * b->terms.size(),
                      cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_counters, sizeof(unsigned int) * kMaxW32);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int) * kStatusWords);
     if (e != cudaSuccess) {
       const int r = cuda_fail((int)e, "bbs_batch_create");
       bbs_batch_destroy(b);
@@ -2106,7 +2137,14 @@ int bbs_batch_run(bbs_batch *b, uint32_t n_steps) {
   BBS_CUDA(cudaEventRecord(b->ev1, b->stream), "event");
   BBS_CUDA(cudaStreamSynchronize(b->stream), "batch run");
   BBS_CUDA(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "event timing");
-  return BBS_OK;
+#ifdef BBS_CHECKED
+  int status[kStatusWords] = {};
+  BBS_CUDA(cudaMemcpy(status, b->d_status, sizeof(status), cudaMemcpyDeviceToHost),
+           "status read");
+  return status_result(status);
+#else
+  return BBS_OK;  // a batch run is never cancelled and checks nothing
+#endif
 }
 
 int bbs_batch_last_run_ms(const bbs_batch *b, float *ms) {

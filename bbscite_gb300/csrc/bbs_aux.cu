@@ -267,6 +267,25 @@ __global__ void __launch_bounds__(256) popc_bench_kernel(int iters,
   }
 }
 
+// A check that fails on purpose: the index 7 is compared with the limit
+// 5 and nothing is read or written at it.
+__global__ void check_selftest_kernel(int *status) {
+  const uint32_t index = 7, limit = 5;
+  if (!device_check(index < limit, status, kCheckSelfTest, index, limit)) return;
+}
+
+int run_check_selftest(int *status_device, int *enabled) {
+#ifdef BBS_CHECKED
+  *enabled = 1;
+#else
+  *enabled = 0;
+#endif
+  check_selftest_kernel<<<1, 32>>>(status_device);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return (int)e;
+}
+
 int run_popc_bench(double *popc_per_s, double *clock_hz) {
   int dev = 0, n_sms = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -15,6 +15,33 @@ namespace bbs {
 #define BBS_FULL_MASK 0xffffffffu
 
 // ------------------------------------------------------------------------
+// Device checks.  A build with BBS_CHECKED defined tests the indices that
+// come from data rather than from loop bounds (the nodes of a realised
+// move, work-list entries, dataset numbers); the first failure sets bit 1
+// of status[0] and stores its code, value and limit in status[1..3], and
+// the caller skips what the index would have reached.  Without
+// BBS_CHECKED every check is true at compile time and costs nothing.
+// ------------------------------------------------------------------------
+__device__ __forceinline__ bool device_check(bool ok, int *status, int code,
+                                             uint32_t value, uint32_t limit) {
+#ifdef BBS_CHECKED
+  if (!ok && status != nullptr && (atomicOr(status, 2) & 2) == 0) {
+    status[1] = code;
+    status[2] = (int)value;
+    status[3] = (int)limit;
+  }
+  return ok;
+#else
+  (void)ok;
+  (void)status;
+  (void)code;
+  (void)value;
+  (void)limit;
+  return true;
+#endif
+}
+
+// ------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11) and the move sampler.  The word
 // assignment matches orc_sample_move in the CPU oracle.
 // ------------------------------------------------------------------------

@@ -11,6 +11,11 @@ namespace bbs {
 // uint64 row -- of which W32 = ceil(n/32) are significant.
 inline constexpr int kMaxW32 = 8;  // 256 nodes
 inline constexpr int kMaxQ = 4;    // cells per lane per chunk
+// Status words of a run: bit 0 of [0] a cancelled run, bit 1 a failed
+// device check (BBS_CHECKED builds) whose code, value and limit are [1..3].
+inline constexpr int kStatusWords = 4;
+inline constexpr int kCheckMoveNode = 1, kCheckUnit = 2, kCheckDataset = 3,
+                     kCheckSelfTest = 4;
 
 __host__ __device__ constexpr int rs_of_w32(int w32) {
   return 2 * ((w32 + 1) / 2);
@@ -93,6 +98,7 @@ struct BatchArgs {
   const uint64_t *chain_off; // [n_chains] word offset of its rows
   const uint32_t *units;     // chains of this launch, costliest first
   int n_units, n_steps;
+  int n_chains, n_datasets;  // bounds of units[] and chain_ds[] entries
   int chains_per_dataset;    // chain c is number c - d * this of dataset d
   uint32_t *rows, *best_rows;
   ChainState *states;
@@ -178,6 +184,10 @@ int launch_score(const ScoreArgs &a, int q, void *stream);
 int launch_apply(const ApplyArgs &a, void *stream);
 int launch_grad(const GradArgs &a, int q, void *stream);
 int run_popc_bench(double *popc_per_s, double *clock_hz);
+// Records one failing device check (code kCheckSelfTest, value 7, limit 5)
+// in status[0..3] without any out-of-range access; 1 when the library was
+// built with device checks (BBS_CHECKED), else 0 and status untouched.
+int run_check_selftest(int *status_device, int *enabled);
 size_t mcmc_smem_bytes(int n_nodes, int wpc, int chains_per_block);
 int pick_q(int n_cells);
 

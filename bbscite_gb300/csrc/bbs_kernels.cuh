@@ -162,6 +162,12 @@ __device__ __forceinline__ void run_chain(
     uint32_t Dv[W32], Dw[W32];
     if (!err_move) {
       const Realized R = realize_move<W32>(cur, n, beta, raw, lane, Dv, Dw);
+      const uint32_t top = max(max(max(R.p.v, R.p.w), max(R.p.parent_of_v, R.p.parent_of_w)),
+                               max(R.p.descendant_of_v, R.p.nondescendant_of_v));
+      if (!device_check(top < (uint32_t)n, status, kCheckMoveNode, top, (uint32_t)n)) {
+        cancelled = true;  // the chain stops where it is
+        break;
+      }
       build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
                           lane);
       scored = prop;
@@ -414,7 +420,13 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
     unit = __shfl_sync(BBS_FULL_MASK, unit, 0);
     if (unit >= (unsigned int)b.n_units) break;
     const uint32_t chain = b.units[unit];
+    if (!device_check(chain < (uint32_t)b.n_chains, b.status, kCheckUnit, chain,
+                      (uint32_t)b.n_chains))
+      continue;
     const uint32_t d = b.chain_ds[chain];
+    if (!device_check(d < (uint32_t)b.n_datasets, b.status, kCheckDataset, d,
+                      (uint32_t)b.n_datasets))
+      continue;
     // The sum score reads the dataset and model tables in place (fewer
     // registers, measured faster); the max score keeps register copies
     // (measured faster there).

@@ -1,8 +1,10 @@
 """ctypes binding of the C ABI in include/bbscite_gb300.h.
 
 The shared library is built in-tree (bbscite_gb300/libbbscite_gb300.so by
-bbscite_gb300/build.py).  There is no fallback: if the library is missing
-or a call fails, a BbsError is raised.
+bbscite_gb300/build.py).  The environment variable BBSCITE_GB300_LIB names
+another build of it to load instead, such as the one with device checks
+(libbbscite_gb300_checked.so).  There is no fallback: if the library is
+missing or a call fails, a BbsError is raised.
 """
 from __future__ import annotations
 
@@ -12,10 +14,11 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(PKG, "libbbscite_gb300.so")
+LIB_PATH = os.environ.get("BBSCITE_GB300_LIB") or os.path.join(
+    PKG, "libbbscite_gb300.so")
 
 BBS_OK, BBS_ERR_INPUT, BBS_ERR_SIZE, BBS_ERR_CUDA, BBS_ERR_TIMEOUT, \
-    BBS_ERR_STATE, BBS_ERR_IO, BBS_ERR_ALLOC = range(8)
+    BBS_ERR_STATE, BBS_ERR_IO, BBS_ERR_ALLOC, BBS_ERR_DEVICE_CHECK = range(9)
 MAX_GENES = 255
 MAX_CELLS = 65535
 
@@ -117,6 +120,7 @@ def lib():
         "bbs_apply_moves": (C.c_int, [v, v, v, u32, v, v, v, v, v]),
         "bbs_sumscore_grad": (C.c_int, [v, v, v, v, u32, v, v, v, v]),
         "bbs_popc_peak": (C.c_int, [v, v]),
+        "bbs_device_check_selftest": (C.c_int, [v, v, v, v]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -44,6 +44,8 @@ extern "C" {
 #define BBS_ERR_STATE 5   /* call order (e.g. run before init_chains) */
 #define BBS_ERR_IO 6      /* file could not be read or written */
 #define BBS_ERR_ALLOC 7   /* host or device allocation failed */
+#define BBS_ERR_DEVICE_CHECK 8 /* a device-side index check failed (builds
+                                  with BBS_CHECKED defined) */
 
 #define BBS_MAX_GENES 255   /* replaces the compile-time 63/95 caps */
 #define BBS_MAX_CELLS 65535 /* integer class totals stay exact in FP32 */
@@ -368,6 +370,19 @@ BBS_API int bbs_score_trees_noalloc(bbs_ctx *ctx, const uint64_t *dm_device,
 
 /* Integer-pipe calibration: 32-bit POPC throughput of this device in
  * operations per second (a timed microbenchmark). */
+/* Device checks (no counterpart in the reference).  A build with
+ * BBS_CHECKED defined (python -m bbscite_gb300.build --checked, giving
+ * libbbscite_gb300_checked.so) tests the device indices that come from
+ * data -- the nodes of every realised move, work-list entries and dataset
+ * numbers -- and skips what a bad index would reach; a run in which a
+ * check failed returns BBS_ERR_DEVICE_CHECK naming the check, the value
+ * and its limit.  bbs_device_check_selftest makes one check fail on
+ * purpose (index 7 against limit 5, no access) and reports what was
+ * recorded: *enabled is 1 in a checked build (then *code = 4, *value = 7,
+ * *limit = 5) and 0 otherwise (nothing recorded, *code = 0). */
+BBS_API int bbs_device_check_selftest(int *enabled, uint32_t *code,
+                                      uint32_t *value, uint32_t *limit);
+
 BBS_API int bbs_popc_peak(double *popc_per_s, double *sm_clock_hz);
 
 #ifdef __cplusplus
