@@ -1759,6 +1759,7 @@ struct bbs_batch {
   // launch groups (row width), rebuilt when the shape changes
   struct Group {
     int w32 = 0, max_nodes = 0;
+    int only_ds = -1;  // the group's dataset when it has only one
     std::vector<uint32_t> units;
     uint32_t *d_units = nullptr;
   };
@@ -1877,6 +1878,9 @@ int batch_build_groups(bbs_batch *b) {
     std::stable_sort(cost.begin(), cost.end(),
                      [](const auto &x, const auto &y) { return x.first > y.first; });
     for (auto &p : cost) g.units.push_back(p.second);
+    g.only_ds = (int)b->chain_ds[g.units[0]];
+    for (const uint32_t u : g.units)
+      if ((int)b->chain_ds[u] != g.only_ds) g.only_ds = -1;
     BBS_CUDA(cudaMalloc(&g.d_units, sizeof(uint32_t) * g.units.size()), "cudaMalloc");
     BBS_CUDA(cudaMemcpy(g.d_units, g.units.data(), sizeof(uint32_t) * g.units.size(),
                         cudaMemcpyHostToDevice), "cudaMemcpy");
@@ -1922,6 +1926,7 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.cancel = nullptr;
     a.status = b->d_status;
     a.max_nodes = grp.max_nodes;
+    a.table_ds = b->sum ? grp.only_ds : -1;
     const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;  // 1, 2 above 128 nodes
     const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");

@@ -10,11 +10,6 @@ int pick_q(int n_cells) {
   return std::min(kMaxQ, std::max(1, (n_cells + 31) / 32));
 }
 
-size_t mcmc_smem_bytes(int n_nodes, int wpc, int cpb) {
-  const int rs = rs_of_w32(w32_of_nodes(n_nodes));
-  return (size_t)cpb * slot_words(n_nodes, rs, wpc) * sizeof(uint32_t);
-}
-
 int launch_mcmc(const RunArgs &a, int q, int cpb, int n_sms, void *stream) {
   const int w32 = w32_of_nodes(a.ds.n_nodes);
   cudaStream_t s = (cudaStream_t)stream;
@@ -38,7 +33,12 @@ int launch_batch(const BatchArgs &b, int w32, int q, bool sum, int wpb,
 template <int W32, bool SUM>
 static int launch_init_t(const InitArgs &a, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32), WPB = 4, Q = 2;
-  const size_t smem = (size_t)WPB * a.max_nodes * RS * sizeof(uint32_t);
+  // per warp: the rows and (sum score) the canonical order and histogram,
+  // as init_kernel lays them out
+  const int n = a.max_nodes;
+  const size_t per_warp = (size_t)4 * n * RS +
+      (SUM ? align16(2 * n) + align16(4 * 32 * ((n + 31) / 32)) : 0);
+  const size_t smem = (size_t)WPB * per_warp;
   auto kern = init_kernel<W32, Q, SUM>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;

@@ -661,12 +661,212 @@ __device__ __forceinline__ float ex2_approx(float t) {
   return r;
 }
 
-template <int W32, int Q>
+// ------------------------------------------------------------------------
+// The sum score's node order.  Every sum-score evaluation adds its per-node
+// terms in one canonical order of the tree -- by depth, ties by node index:
+// the root first, every node after its parent -- and in the same pairs, so
+// that a cell's sum does not depend on where it is computed (cells held in
+// registers or streamed, any launch shape, batched or alone) nor on how its
+// counts are found.  Two count sources give the same integers:
+//   - masked popcounts of the node's ancestor row (any tree);
+//   - inherited counts: a node's ancestors are its parent's plus itself,
+//     so (d, m) of node j = (d, m) of its parent + (D, M) bits of gene j.
+//     This needs the tree's parent vector, a per-warp table of every
+//     node's packed counts and a block table of per-gene increments, and
+//     issues no POPC; it serves cells held in registers with rows of up to
+//     four words.
+// ------------------------------------------------------------------------
+struct SumCtx {
+  uint16_t *ord;        // [n]: node | parent << 8, in canonical order
+  int *hist;            // [32 * ceil(n / 32)]: depth histogram, scratch
+  uint16_t *cnt;        // [n][Q][32]: packed counts d | m << 8, or null
+  const uint16_t *inc;  // [n][inc_stride]: per-gene increments, or null
+  int inc_stride;       // cell slots per increment row
+  const uint8_t *par;   // parent vector of the evaluated tree, or null
+};
+
+// ord and hist of the tree with ancestor rows `rows`; the parent of each
+// node from `par` (0 where par is null).  Depth = ancestors - 1 = the
+// popcount of the node's row less one (a row holds the node and the root).
+template <int W32>
+__device__ __forceinline__ void canonical_order(const uint32_t *rows, int n,
+                                                const uint8_t *par,
+                                                uint16_t *ord, int *hist,
+                                                int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  const int B = (n + 31) >> 5;  // node groups; bins per lane in the scan
+  for (int i = lane; i < 32 * B; i += 32) hist[i] = 0;
+  __syncwarp();
+  int dep[W32];
+#pragma unroll
+  for (int g = 0; g < W32; g++) {
+    const int x = 32 * g + lane;
+    dep[g] = -1;
+    if (x < n) {
+      uint32_t a[W32];
+      ld_row<W32>(rows + x * RS, a);
+      int pc = 0;
+#pragma unroll
+      for (int k = 0; k < W32; k++) pc += __popc(a[k]);
+      dep[g] = pc - 1;
+      atomicAdd(&hist[pc - 1], 1);
+    }
+  }
+  __syncwarp();
+  // exclusive scan of the bins, lane l owning bins l*B .. l*B + B - 1
+  int loc[W32], s = 0;
+#pragma unroll
+  for (int k = 0; k < W32; k++) {
+    loc[k] = k < B ? hist[lane * B + k] : 0;
+    s += loc[k];
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(BBS_FULL_MASK, incl, o);
+    if (lane >= o) incl += v;
+  }
+  int run = incl - s;
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < W32; k++)
+    if (k < B) {
+      hist[lane * B + k] = run;
+      run += loc[k];
+    }
+  __syncwarp();
+  const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+  for (int g = 0; g < W32; g++) {
+    const int x = 32 * g + lane;
+    const bool valid = x < n;
+    const unsigned same = __match_any_sync(BBS_FULL_MASK, valid ? dep[g] : -1);
+    if (valid) {
+      const int pos = hist[dep[g]] + __popc(same & below);
+      ord[pos] = (uint16_t)(x | ((par != nullptr ? (int)par[x] : 0) << 8));
+    }
+    __syncwarp();
+    if (valid && (same & below) == 0) hist[dep[g]] += __popc(same);
+    __syncwarp();
+  }
+}
+
+// The parent vector of the tree with ancestor rows `rows`: each node's
+// deepest proper ancestor (the root is its own parent).  depth_tmp: n ints.
+template <int W32>
+__device__ __forceinline__ void derive_parents(const uint32_t *rows, int n,
+                                               uint8_t *par, int *depth_tmp,
+                                               int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  for (int x = lane; x < n; x += 32) {
+    uint32_t a[W32];
+    ld_row<W32>(rows + x * RS, a);
+    int pc = 0;
+#pragma unroll
+    for (int k = 0; k < W32; k++) pc += __popc(a[k]);
+    depth_tmp[x] = pc;
+  }
+  __syncwarp();
+  for (int x = lane; x < n; x += 32) {
+    uint32_t a[W32];
+    ld_row<W32>(rows + x * RS, a);
+    int best = x, bd = -1;
+#pragma unroll
+    for (int k = 0; k < W32; k++) {
+      uint32_t w = k == (x >> 5) ? a[k] & ~(1u << (x & 31)) : a[k];
+      while (w != 0u) {  // at most 32 set bits
+        const int y = 32 * k + __ffs(w) - 1;
+        w &= w - 1u;
+        if (depth_tmp[y] > bd) {
+          bd = depth_tmp[y];
+          best = y;
+        }
+      }
+    }
+    par[x] = (uint8_t)best;
+  }
+  __syncwarp();
+}
+
+// The proposal's parent vector from the current one and the realised move,
+// as the reference's own test restates each move on parent vectors
+// (test/MutationTree.cpp:697-735).  `related`: w is an ancestor of v.
+__device__ __forceinline__ void propose_parents(const uint8_t *cur,
+                                                uint8_t *prop, int n,
+                                                const bbs_move_params &p,
+                                                bool related, int lane) {
+  const uint32_t v = p.v, w = p.w;
+  const bool swap_nodes = p.move_type == BBS_MOVE_SWAP_NODES;
+  for (int x = lane; x < n; x += 32) {
+    uint32_t q = cur[x];
+    if (swap_nodes && (uint32_t)x != v && (uint32_t)x != w)
+      q = q == v ? w : (q == w ? v : q);
+    prop[x] = (uint8_t)q;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    if (p.move_type == BBS_MOVE_PRUNE_REATTACH) {
+      prop[v] = (uint8_t)p.nondescendant_of_v;
+    } else if (swap_nodes) {
+      const uint32_t pv = cur[v], pw = cur[w];
+      if (pv == w) {
+        prop[v] = (uint8_t)pw;
+        prop[w] = (uint8_t)v;
+      } else if (pw == v) {
+        prop[w] = (uint8_t)pv;
+        prop[v] = (uint8_t)w;
+      } else {
+        prop[v] = (uint8_t)pw;
+        prop[w] = (uint8_t)pv;
+      }
+    } else if (p.move_type == BBS_MOVE_SWAP_SUBTREES) {
+      prop[v] = (uint8_t)p.parent_of_w;
+      prop[w] = (uint8_t)(related ? p.descendant_of_v : p.parent_of_v);
+    }
+  }
+  __syncwarp();
+}
+
+// Checked builds: every non-root node's row is its parent's row plus the
+// node itself.
+template <int W32>
+__device__ __forceinline__ bool parents_match_rows(const uint32_t *rows, int n,
+                                                   const uint8_t *par,
+                                                   int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  bool ok = true;
+  for (int x = lane; x < n - 1; x += 32) {
+    const int p = par[x];
+    if (p >= n) {
+      ok = false;
+      continue;
+    }
+    uint32_t a[W32], b[W32];
+    ld_row<W32>(rows + x * RS, a);
+    ld_row<W32>(rows + p * RS, b);
+#pragma unroll
+    for (int k = 0; k < W32; k++) {
+      const uint32_t own = k == (x >> 5) ? 1u << (x & 31) : 0u;
+      ok = ok && a[k] == (b[k] | own) && (b[k] & own) == 0u;
+    }
+  }
+  return __all_sync(BBS_FULL_MASK, ok);
+}
+
+// The increments of the block table for cell slot `slot` (cells
+// c0 + stride * q + lane index the table directly).
+__device__ __forceinline__ uint32_t gene_increment(const SumCtx &sx, int j,
+                                                   int slot) {
+  return sx.inc[j * sx.inc_stride + slot];
+}
+
+template <int W32, int Q, bool INHERIT>
 __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const Cells<W32, Q> &cb,
                                           const LogTable &L, int c0, int stride,
                                           int lane, int n_cells,
-                                          long long (&acc)[6]) {
+                                          long long (&acc)[6],
+                                          const SumCtx &sx) {
   constexpr int RS = rs_of_w32(W32);
   const float c1 = (L.l01 - L.l00) * kLog2E;  // per counted observed-0 bit
   const float c2 = (L.l11 - L.l10) * kLog2E;  // per counted observed-1 bit
@@ -677,44 +877,100 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
     r[q] = fmaf(pd, u0, pm * u1) - 72.0f;
     base[q] = (fmaf(pd, L.l00, pm * L.l10) - r[q]) * kLog2E;
-    mx[q] = -INFINITY;
-    z[q] = ed[q] = em[q] = 0.0f;
   }
-  // two nodes per iteration: independent work for the scheduler
-  int j = 0;
+  // the root (ord[0]) has no counted bits: t = base
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    if constexpr (INHERIT) sx.cnt[(((int)(sx.ord[0] & 0xFF)) * Q + q) * 32 + lane] = 0;
+    mx[q] = base[q];
+    z[q] = ex2_approx(base[q]);
+    ed[q] = em[q] = 0.0f;
+  }
+  // the other nodes two at a time: independent work for the scheduler
+  int i = 1;
 #pragma unroll 1
-  for (; j + 1 < n; j += 2) {
-    uint32_t a[W32], b[W32];
-    ld_row<W32>(rows + j * RS, a);
-    ld_row<W32>(rows + (j + 1) * RS, b);
+  for (; i + 1 < n; i += 2) {
+    const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
+    const int j0 = (int)(o0 & 0xFF), j1 = (int)(o1 & 0xFF);
+    float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
+    if constexpr (INHERIT) {
+      const int p0 = (int)(o0 >> 8), p1 = (int)(o1 >> 8);
+      uint32_t k0[Q], k1[Q];
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        k0[q] = (uint32_t)sx.cnt[(p0 * Q + q) * 32 + lane] +
+                gene_increment(sx, j0, c0 + stride * q + lane);
+        sx.cnt[(j0 * Q + q) * 32 + lane] = (uint16_t)k0[q];
+      }
+      // node j1 may be j0's child: its parent's counts are read after
+      // they are stored
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        k1[q] = (uint32_t)sx.cnt[(p1 * Q + q) * 32 + lane] +
+                gene_increment(sx, j1, c0 + stride * q + lane);
+        sx.cnt[(j1 * Q + q) * 32 + lane] = (uint16_t)k1[q];
+      }
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        fd0[q] = __int_as_float(0x4B000000 | (k0[q] & 0xFFu)) - 8388608.0f;
+        fm0[q] = __int_as_float(0x4B000000 | (k0[q] >> 8)) - 8388608.0f;
+        fd1[q] = __int_as_float(0x4B000000 | (k1[q] & 0xFFu)) - 8388608.0f;
+        fm1[q] = __int_as_float(0x4B000000 | (k1[q] >> 8)) - 8388608.0f;
+      }
+    } else {
+      uint32_t a[W32], b[W32];
+      ld_row<W32>(rows + j0 * RS, a);
+      ld_row<W32>(rows + j1 * RS, b);
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        fd0[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+        fm0[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+        fd1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
+        fm1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
+      }
+    }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      const float fd0 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
-      const float fm0 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
-      const float fd1 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
-      const float fm1 = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
-      const float t0 = fmaf(fd0, c1, fmaf(fm0, c2, base[q]));
-      const float t1 = fmaf(fd1, c1, fmaf(fm1, c2, base[q]));
+      const float t0 = fmaf(fd0[q], c1, fmaf(fm0[q], c2, base[q]));
+      const float t1 = fmaf(fd1[q], c1, fmaf(fm1[q], c2, base[q]));
       const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
       mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
       z[q] += e0 + e1;
-      ed[q] = fmaf(e0, fd0, fmaf(e1, fd1, ed[q]));
-      em[q] = fmaf(e0, fm0, fmaf(e1, fm1, em[q]));
+      ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
+      em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
     }
   }
-  if (j < n) {
-    uint32_t a[W32];
-    ld_row<W32>(rows + j * RS, a);
+  if (i < n) {
+    const uint32_t o = sx.ord[i];
+    const int j = (int)(o & 0xFF);
+    float fd[Q], fm[Q];
+    if constexpr (INHERIT) {
+      const int p = (int)(o >> 8);
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        const uint32_t k = (uint32_t)sx.cnt[(p * Q + q) * 32 + lane] +
+                           gene_increment(sx, j, c0 + stride * q + lane);
+        sx.cnt[(j * Q + q) * 32 + lane] = (uint16_t)k;
+        fd[q] = __int_as_float(0x4B000000 | (k & 0xFFu)) - 8388608.0f;
+        fm[q] = __int_as_float(0x4B000000 | (k >> 8)) - 8388608.0f;
+      }
+    } else {
+      uint32_t a[W32];
+      ld_row<W32>(rows + j * RS, a);
+#pragma unroll
+      for (int q = 0; q < Q; q++) {
+        fd[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+        fm[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+      }
+    }
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      const float fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
-      const float fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
-      const float t = fmaf(fd, c1, fmaf(fm, c2, base[q]));
+      const float t = fmaf(fd[q], c1, fmaf(fm[q], c2, base[q]));
       const float e = ex2_approx(t);
       mx[q] = fmaxf(mx[q], t);
       z[q] += e;
-      ed[q] = fmaf(e, fd, ed[q]);
-      em[q] = fmaf(e, fm, em[q]);
+      ed[q] = fmaf(e, fd[q], ed[q]);
+      em[q] = fmaf(e, fm[q], em[q]);
     }
   }
   bool bad[Q], any = false;
@@ -724,6 +980,8 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     any |= bad[q];
   }
   if (__any_sync(BBS_FULL_MASK, any)) {
+    // cells summed once more against their maximum, one node at a time in
+    // the same order
 #pragma unroll
     for (int q = 0; q < Q; q++)
       if (bad[q]) {
@@ -733,14 +991,22 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
         z[q] = ed[q] = em[q] = 0.0f;
       }
 #pragma unroll 1
-    for (int j = 0; j < n; j++) {
+    for (int i2 = 0; i2 < n; i2++) {
+      const int j = (int)(sx.ord[i2] & 0xFF);
       uint32_t a[W32];
-      ld_row<W32>(rows + j * RS, a);
+      if constexpr (!INHERIT) ld_row<W32>(rows + j * RS, a);
 #pragma unroll
       for (int q = 0; q < Q; q++) {
         if (!bad[q]) continue;
-        const float fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
-        const float fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+        float fd, fm;
+        if constexpr (INHERIT) {
+          const uint32_t k = sx.cnt[(j * Q + q) * 32 + lane];
+          fd = __int_as_float(0x4B000000 | (k & 0xFFu)) - 8388608.0f;
+          fm = __int_as_float(0x4B000000 | (k >> 8)) - 8388608.0f;
+        } else {
+          fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+          fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+        }
         const float e = ex2_approx(fmaf(fd, c1, fmaf(fm, c2, base[q])));
         z[q] += e;
         ed[q] = fmaf(e, fd, ed[q]);
@@ -765,24 +1031,37 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
 }
 
 // This warp's part of the sum score and expected counts (fixed point,
-// warp-reduced).
+// warp-reduced), its terms added in the canonical order (sx.ord, built
+// here).  Inherited counts serve cells held in registers when sx brings the
+// parent vector, the count table and the increment table.
 template <int W32, int Q>
 __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
                                          const DatasetDev &ds,
                                          Cells<W32, Q> &cb, bool resident,
                                          const LogTable &L, int wpc, int wic,
-                                         int lane, long long (&acc)[6]) {
+                                         int lane, long long (&acc)[6],
+                                         const SumCtx &sx) {
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = 0;
+  canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
   if (resident) {
-    sum_cells<W32, Q>(rows, n, cb, L, 32 * wic, 32 * wpc, lane, ds.n_cells,
-                      acc);
+    bool inherit = false;
+    if constexpr (W32 <= 4)
+      inherit = sx.cnt != nullptr && sx.inc != nullptr && sx.par != nullptr;
+    if (inherit) {
+      if constexpr (W32 <= 4)
+        sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
+                                ds.n_cells, acc, sx);
+    } else {
+      sum_cells<W32, Q, false>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
+                               ds.n_cells, acc, sx);
+    }
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      sum_cells<W32, Q>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc, lane,
-                        ds.n_cells, acc);
+      sum_cells<W32, Q, false>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc, lane,
+                               ds.n_cells, acc, sx);
     }
   }
 #pragma unroll

@@ -15,7 +15,7 @@ inline constexpr int kMaxQ = 4;    // cells per lane per chunk
 // device check (BBS_CHECKED builds) whose code, value and limit are [1..3].
 inline constexpr int kStatusWords = 4;
 inline constexpr int kCheckMoveNode = 1, kCheckUnit = 2, kCheckDataset = 3,
-                     kCheckSelfTest = 4;
+                     kCheckSelfTest = 4, kCheckParent = 5;
 
 __host__ __device__ constexpr int rs_of_w32(int w32) {
   return 2 * ((w32 + 1) / 2);
@@ -106,6 +106,8 @@ struct BatchArgs {
   const volatile int *cancel;
   int *status;
   int max_nodes;             // shared memory is sized for this
+  int table_ds;              // the launch's only dataset (sum score:
+                             // inherited counts), or -1
 };
 
 // Initial state of each chain: evaluate its tree at (alpha_mean,
@@ -188,7 +190,6 @@ int run_popc_bench(double *popc_per_s, double *clock_hz);
 // in status[0..3] without any out-of-range access; 1 when the library was
 // built with device checks (BBS_CHECKED), else 0 and status untouched.
 int run_check_selftest(int *status_device, int *enabled);
-size_t mcmc_smem_bytes(int n_nodes, int wpc, int chains_per_block);
 int pick_q(int n_cells);
 
 }  // namespace bbs

@@ -40,11 +40,72 @@ __device__ __forceinline__ void copy_rows(const uint32_t *src, uint32_t *dst,
   copy_rows_part<W32>(src, dst, n, 1, 0, lane);
 }
 
-// Shared-memory words per chain slot: two row buffers, the partial sums
-// of both step parities (2 x wpc x 12 words) and a flag word, padded to
-// 16 bytes.
-__host__ __device__ inline int slot_words(int n, int rs, int wpc) {
-  return 2 * n * rs + 24 * wpc + 4;
+// Shared memory of the chain kernels, in bytes (16-byte aligned pieces).
+__host__ __device__ inline int align16(int b) { return (b + 15) & ~15; }
+
+// Per warp of a sum-score chain: the canonical node order, its depth
+// histogram and (rows of up to four words) the packed counts of every node
+// for the lane's cells.
+__host__ __device__ inline int sum_warp_bytes(int n, int w32, int q) {
+  return align16(2 * n) + align16(4 * 32 * ((n + 31) / 32)) +
+         (w32 <= 4 ? align16(2 * n * q * 32) : 0);
+}
+
+// One chain slot: two row buffers, the partial sums of both step parities
+// (2 x wpc x 12 words) and a flag word; for the sum score, the current and
+// proposed parent vectors and each warp's sum scratch.
+__host__ __device__ inline int slot_bytes(int n, int rs, int wpc, bool sum,
+                                          int w32, int q) {
+  int b = 4 * (2 * n * rs + 24 * wpc + 4);
+  if (sum) b += align16(2 * n) + wpc * sum_warp_bytes(n, w32, q);
+  return b;
+}
+
+// After the slots: the block's table of per-gene increments (sum score,
+// rows of up to four words) for its 32 * q * wpc resident cell slots.
+__host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
+                                           bool sum) {
+  return sum && w32 <= 4 ? align16(2 * n * 32 * q * wpc) : 0;
+}
+
+// The sum-score pieces of a slot: parent vectors and warp wic's scratch.
+struct SlotSum {
+  uint8_t *par0, *par1;
+  SumCtx sx;
+};
+
+__device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n, int rs,
+                                            int wpc, int wic, int w32, int q) {
+  SlotSum o{};
+  uint8_t *p = slot + 4 * (2 * n * rs + 24 * wpc + 4);
+  o.par0 = p;
+  o.par1 = p + n;
+  p += align16(2 * n) + wic * sum_warp_bytes(n, w32, q);
+  o.sx.ord = reinterpret_cast<uint16_t *>(p);
+  p += align16(2 * n);
+  o.sx.hist = reinterpret_cast<int *>(p);
+  p += align16(4 * 32 * ((n + 31) / 32));
+  o.sx.cnt = w32 <= 4 ? reinterpret_cast<uint16_t *>(p) : nullptr;
+  return o;
+}
+
+// The block's increment table: gene j of cell slot c (cell c of the
+// dataset; zero past its cells) is D | M << 8 of that gene.  Cell rows are
+// read with the stride rs that load_cells uses.
+__device__ __forceinline__ void build_increments(uint16_t *table, int stride,
+                                                 const DatasetDev &ds, int rs) {
+  const int n = ds.n_nodes;
+  for (int idx = threadIdx.x; idx < n * stride; idx += blockDim.x) {
+    const int j = idx / stride, c = idx - j * stride;
+    uint32_t v = 0;
+    if (c < ds.n_cells) {
+      const uint32_t k = __ldg(ds.K + (size_t)c * rs + (j >> 5));
+      const uint32_t m = __ldg(ds.M + (size_t)c * rs + (j >> 5));
+      const uint32_t b = 1u << (j & 31);
+      v = ((k & ~m & b) ? 1u : 0u) | ((m & b) ? 256u : 0u);
+    }
+    table[idx] = (uint16_t)v;
+  }
 }
 
 // Evaluates a tree for the whole chain (all wpc warps): returns the score
@@ -58,6 +119,7 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
                                           const LogTable &L, float prior,
                                           int wpc, int wic, int lane,
                                           int *part, int parity,
+                                          const SumCtx &sx,
                                           float (&e)[4], int &sk, int &sm,
                                           float &smax) {
   if constexpr (!SUM) {
@@ -86,7 +148,7 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
     return smax;
   } else {
     long long acc[6];
-    sum_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, acc);
+    sum_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, acc, sx);
     if (wpc > 1) {
       long long *pp = reinterpret_cast<long long *>(part) + parity * 6 * wpc;
       if (lane == 0)
@@ -114,14 +176,26 @@ __device__ __forceinline__ void run_chain(
     ChainState *gstate,
     const bbs_raw_move *moves, bbs_step_trace *trace, int n_steps,
     const volatile int *cancel, int *status, uint32_t *buf0, uint32_t *buf1,
-    int *part, volatile int *sflag, Cells<W32, Q> &cb, bool resident, int wpc,
-    int wic, int lane) {
+    int *part, volatile int *sflag, const SlotSum &ss, Cells<W32, Q> &cb,
+    bool resident, int wpc, int wic, int lane) {
   const int n = ds.n_nodes;
   const bool multi = wpc > 1;
   const ChainState st = *gstate;
   copy_rows_part<W32>(g, buf0, n, wpc, wic, lane);
   if (multi) __syncthreads(); else __syncwarp();
   uint32_t *cur = buf0, *prop = buf1;
+  // Sum score with inherited counts: the parent vectors of the current tree
+  // and of the proposal follow the rows.
+  uint8_t *cpar = nullptr, *ppar = nullptr;
+  if constexpr (SUM && W32 <= 4) {
+    if (ss.sx.inc != nullptr && resident) {
+      cpar = ss.par0;
+      ppar = ss.par1;
+      if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
+      if (multi) __syncthreads(); else __syncwarp();
+    }
+  }
+  SumCtx sx = ss.sx;
   float alpha = st.alpha, beta = st.beta, score = st.score, prior = st.prior;
   LogTable L{st.l00, st.l10, st.l01, st.l11};
   float ec[4] = {st.ec[0], st.ec[1], st.ec[2], st.ec[3]};
@@ -170,6 +244,8 @@ __device__ __forceinline__ void run_chain(
       }
       build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
                           lane);
+      if (cpar != nullptr && wic == 0)
+        propose_parents(cpar, ppar, n, R.p, R.related, lane);
       scored = prop;
       // src/Application.hpp:443-450
       if (raw.move_type == BBS_MOVE_SWAP_SUBTREES && R.related)
@@ -202,11 +278,23 @@ __device__ __forceinline__ void run_chain(
       beta_terms_f(ds, pbeta, PL.l01, PL.l11, pprior);
     }
     if (multi) __syncthreads(); else __syncwarp();
+    sx.par = cpar == nullptr ? nullptr : (scored == cur ? cpar : ppar);
+#ifdef BBS_CHECKED
+    if constexpr (SUM && W32 <= 4) {
+      // the proposal's parent vector against its rows (value: move type)
+      if (cpar != nullptr && scored != cur &&
+          !device_check(parents_match_rows<W32>(scored, n, ppar, lane), status,
+                        kCheckParent, (uint32_t)raw.move_type, 4u)) {
+        cancelled = true;  // the chain stops where it is
+        break;
+      }
+    }
+#endif
     float e[4], psmax;
     int sk, sm;
     const float pscore = evaluate<W32, Q, SUM>(scored, n, ds, cb, resident, PL,
                                                pprior, wpc, wic, lane, part,
-                                               i & 1, e, sk, sm, psmax);
+                                               i & 1, sx, e, sk, sm, psmax);
     bool accept;
     if (err_move && learn) {
       const ErrorGeom pgeo = error_geometry(ds, palpha, pbeta, md.gamma, e);
@@ -284,6 +372,9 @@ __device__ __forceinline__ void run_chain(
         uint32_t *t = cur;
         cur = prop;
         prop = t;
+        uint8_t *tp = cpar;
+        cpar = ppar;
+        ppar = tp;
       }
       alpha = palpha;
       beta = pbeta;
@@ -351,13 +442,29 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   const int cpb = wpb / wpc;
   const int slot = wib / wpc, wic = wib - slot * wpc;
   const int n = a.ds.n_nodes;
-  uint32_t *buf0 = smem + (size_t)slot * slot_words(n, RS, wpc);
+  const int sb = slot_bytes(n, RS, wpc, SUM, W32, Q);
+  uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)slot * sb;
+  uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   uint32_t *buf1 = buf0 + n * RS;
   int *part = reinterpret_cast<int *>(buf0 + 2 * n * RS);
   volatile int *sflag = part + 24 * wpc;
   const bool resident = a.ds.n_cells <= 32 * wpc * Q;
   Cells<W32, Q> cb;
   if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
+  SlotSum ss{};
+  if constexpr (SUM) {
+    ss = slot_sum(slot_base, n, RS, wpc, wic, W32, Q);
+    if constexpr (W32 <= 4) {
+      if (resident) {  // the same for the whole block
+        uint16_t *table = reinterpret_cast<uint16_t *>(
+            reinterpret_cast<uint8_t *>(smem) + (size_t)cpb * sb);
+        build_increments(table, 32 * Q * wpc, a.ds, RS);
+        __syncthreads();
+        ss.sx.inc = table;
+        ss.sx.inc_stride = 32 * Q * wpc;
+      }
+    }
+  }
   for (int chain = blockIdx.x * cpb + slot; chain < a.n_chains;
        chain += gridDim.x * cpb) {
     const bbs_raw_move *moves = nullptr;
@@ -373,8 +480,8 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
         K > 1 ? a.list_hash + (size_t)chain * K : nullptr,
         K > 1 ? a.list_beta + (size_t)chain * K : nullptr, K, a.states + chain,
         moves, trace,
-        a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, cb, resident,
-        wpc, wic, lane);
+        a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, ss, cb,
+        resident, wpc, wic, lane);
   }
 }
 
@@ -385,6 +492,7 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
                                            const ModelDev &md, uint32_t chain,
                                            uint32_t d, uint32_t *buf0,
                                            int *part, volatile int *sflag,
+                                           const SlotSum &ss_in,
                                            Cells<W32, Q> &cb, int lane) {
   constexpr int RS = rs_of_w32(W32);
   // the dataset's node count is within this launch's row width
@@ -395,10 +503,13 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
   // Philox key: the chain's number within its dataset, so a dataset's
   // chains draw the same moves here as in a one-dataset run.
   const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
+  // the increment table holds the cells of dataset b.table_ds only
+  SlotSum ss = ss_in;
+  if ((int)d != b.table_ds) ss.sx.inc = nullptr;
   run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
                          nullptr, nullptr, 1, b.states + chain, nullptr,
                          nullptr, b.n_steps, b.cancel, b.status, buf0, buf1,
-                         part, sflag, cb, resident, 1, 0, lane);
+                         part, sflag, ss, cb, resident, 1, 0, lane);
 }
 
 // Many datasets: warps take chains from a shared work list (costliest
@@ -410,9 +521,27 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   constexpr int RS = rs_of_w32(W32);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  uint32_t *buf0 = smem + (size_t)wib * slot_words(b.max_nodes, RS, 1);
+  const int sb = slot_bytes(b.max_nodes, RS, 1, SUM, W32, Q);
+  uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)wib * sb;
+  uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
   volatile int *sflag = part + 24;
+  SlotSum ss{};
+  if constexpr (SUM) {
+    ss = slot_sum(slot_base, b.max_nodes, RS, 1, 0, W32, Q);
+    if constexpr (W32 <= 4) {
+      // one dataset in this launch with its cells in registers: the block's
+      // increment table (the same decision in every thread of the block)
+      if (b.table_ds >= 0 && b.ds[b.table_ds].n_cells <= 32 * Q) {
+        uint16_t *table = reinterpret_cast<uint16_t *>(
+            reinterpret_cast<uint8_t *>(smem) + (size_t)(blockDim.x >> 5) * sb);
+        build_increments(table, 32 * Q, b.ds[b.table_ds], RS);
+        __syncthreads();
+        ss.sx.inc = table;
+        ss.sx.inc_stride = 32 * Q;
+      }
+    }
+  }
   Cells<W32, Q> cb;
   for (;;) {
     unsigned int unit = 0;
@@ -432,11 +561,11 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
     // (measured faster there).
     if constexpr (SUM) {
       batch_unit<W32, Q, SUM>(b, b.ds[d], b.md[d], chain, d, buf0, part,
-                              sflag, cb, lane);
+                              sflag, ss, cb, lane);
     } else {
       const DatasetDev ds = b.ds[d];
       const ModelDev md = b.md[d];
-      batch_unit<W32, Q, SUM>(b, ds, md, chain, d, buf0, part, sflag, cb,
+      batch_unit<W32, Q, SUM>(b, ds, md, chain, d, buf0, part, sflag, ss, cb,
                               lane);
     }
   }
@@ -459,7 +588,17 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
   const int n = ds.n_nodes;
   const uint64_t off = a.chain_off != nullptr ? a.chain_off[chain]
                                               : (uint64_t)chain * n * RS;
-  uint32_t *rows = smem + (size_t)wib * a.max_nodes * RS;
+  // per warp: the tree's rows, then (sum score) the canonical order and
+  // its histogram
+  const int wb = 4 * a.max_nodes * RS +
+                 (SUM ? align16(2 * a.max_nodes) + align16(4 * 32 * ((a.max_nodes + 31) / 32)) : 0);
+  uint8_t *mine = reinterpret_cast<uint8_t *>(smem) + (size_t)wib * wb;
+  uint32_t *rows = reinterpret_cast<uint32_t *>(mine);
+  SumCtx sx{};
+  if constexpr (SUM) {
+    sx.ord = reinterpret_cast<uint16_t *>(mine + 4 * a.max_nodes * RS);
+    sx.hist = reinterpret_cast<int *>(mine + 4 * a.max_nodes * RS + align16(2 * a.max_nodes));
+  }
   copy_rows<W32>(a.rows + off, rows, n, lane);
   __syncwarp();
   const float *tm = a.terms + 8 * (size_t)d;
@@ -469,7 +608,7 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
   float e[4], smax;
   int sk, sm;
   const float S = evaluate<W32, Q, SUM>(rows, n, ds, cb, false, L, prior, 1, 0,
-                                        lane, nullptr, 0, e, sk, sm, smax);
+                                        lane, nullptr, 0, sx, e, sk, sm, smax);
   if (lane == 0) {
     ChainState o;
     o.alpha = alpha;
