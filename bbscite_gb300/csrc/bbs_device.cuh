@@ -860,6 +860,67 @@ __device__ __forceinline__ uint32_t gene_increment(const SumCtx &sx, int j,
   return sx.inc[j * sx.inc_stride + slot];
 }
 
+// The float work of two nodes for the lane's cells (both count sources
+// share it, so the sums are the same whichever found the counts).
+template <int Q>
+__device__ __forceinline__ void sum_pair(const float (&fd0)[Q],
+                                         const float (&fm0)[Q],
+                                         const float (&fd1)[Q],
+                                         const float (&fm1)[Q], float c1,
+                                         float c2, const float (&base)[Q],
+                                         float (&mx)[Q], float (&z)[Q],
+                                         float (&ed)[Q], float (&em)[Q]) {
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const float t0 = fmaf(fd0[q], c1, fmaf(fm0[q], c2, base[q]));
+    const float t1 = fmaf(fd1[q], c1, fmaf(fm1[q], c2, base[q]));
+    const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
+    mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
+    z[q] += e0 + e1;
+    ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
+    em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
+  }
+}
+
+// Inherited counts of the nodes at order positions i and i + 1, stored in
+// the count table.  All four loads come first; when node i + 1 is node i's
+// child, its parent's counts are taken from the register instead of the
+// table (whose entry is not stored yet).
+template <int Q>
+__device__ __forceinline__ void inherit_pair(const SumCtx &sx, int i, int c0,
+                                             int stride, int lane,
+                                             uint32_t (&k0)[Q],
+                                             uint32_t (&k1)[Q]) {
+  const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
+  const int j0 = (int)(o0 & 0xFF), p0 = (int)(o0 >> 8);
+  const int j1 = (int)(o1 & 0xFF), p1 = (int)(o1 >> 8);
+  uint32_t a0[Q], a1[Q], g0[Q], g1[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    a0[q] = sx.cnt[(p0 * Q + q) * 32 + lane];
+    a1[q] = sx.cnt[(p1 * Q + q) * 32 + lane];
+    g0[q] = gene_increment(sx, j0, c0 + stride * q + lane);
+    g1[q] = gene_increment(sx, j1, c0 + stride * q + lane);
+  }
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    k0[q] = a0[q] + g0[q];
+    k1[q] = (p1 == j0 ? k0[q] : a1[q]) + g1[q];
+    sx.cnt[(j0 * Q + q) * 32 + lane] = (uint16_t)k0[q];
+    sx.cnt[(j1 * Q + q) * 32 + lane] = (uint16_t)k1[q];
+  }
+}
+
+template <int Q>
+__device__ __forceinline__ void counts_to_float(const uint32_t (&k)[Q],
+                                                float (&fd)[Q], float (&fm)[Q]) {
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    fd[q] = __int_as_float(0x4B000000 | (k[q] & 0xFFu)) - 8388608.0f;
+    fm[q] = __int_as_float(0x4B000000 | (k[q] >> 8)) - 8388608.0f;
+  }
+}
+
 template <int W32, int Q, bool INHERIT>
 __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const Cells<W32, Q> &cb,
@@ -888,36 +949,36 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
   }
   // the other nodes two at a time: independent work for the scheduler
   int i = 1;
-#pragma unroll 1
-  for (; i + 1 < n; i += 2) {
-    const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
-    const int j0 = (int)(o0 & 0xFF), j1 = (int)(o1 & 0xFF);
-    float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
-    if constexpr (INHERIT) {
-      const int p0 = (int)(o0 >> 8), p1 = (int)(o1 >> 8);
+  if constexpr (INHERIT) {
+    // counts one pair ahead of the float work, which hides the table's
+    // load latency behind the previous pair's arithmetic
+    if (i + 1 < n) {
       uint32_t k0[Q], k1[Q];
+      inherit_pair<Q>(sx, i, c0, stride, lane, k0, k1);
+#pragma unroll 1
+      for (; i + 1 < n; i += 2) {
+        uint32_t n0[Q], n1[Q];
+        const bool more = i + 3 < n;
+        if (more) inherit_pair<Q>(sx, i + 2, c0, stride, lane, n0, n1);
+        float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
+        counts_to_float<Q>(k0, fd0, fm0);
+        counts_to_float<Q>(k1, fd1, fm1);
+        sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+        if (more) {
 #pragma unroll
-      for (int q = 0; q < Q; q++) {
-        k0[q] = (uint32_t)sx.cnt[(p0 * Q + q) * 32 + lane] +
-                gene_increment(sx, j0, c0 + stride * q + lane);
-        sx.cnt[(j0 * Q + q) * 32 + lane] = (uint16_t)k0[q];
+          for (int q = 0; q < Q; q++) {
+            k0[q] = n0[q];
+            k1[q] = n1[q];
+          }
+        }
       }
-      // node j1 may be j0's child: its parent's counts are read after
-      // they are stored
-#pragma unroll
-      for (int q = 0; q < Q; q++) {
-        k1[q] = (uint32_t)sx.cnt[(p1 * Q + q) * 32 + lane] +
-                gene_increment(sx, j1, c0 + stride * q + lane);
-        sx.cnt[(j1 * Q + q) * 32 + lane] = (uint16_t)k1[q];
-      }
-#pragma unroll
-      for (int q = 0; q < Q; q++) {
-        fd0[q] = __int_as_float(0x4B000000 | (k0[q] & 0xFFu)) - 8388608.0f;
-        fm0[q] = __int_as_float(0x4B000000 | (k0[q] >> 8)) - 8388608.0f;
-        fd1[q] = __int_as_float(0x4B000000 | (k1[q] & 0xFFu)) - 8388608.0f;
-        fm1[q] = __int_as_float(0x4B000000 | (k1[q] >> 8)) - 8388608.0f;
-      }
-    } else {
+    }
+  } else {
+#pragma unroll 1
+    for (; i + 1 < n; i += 2) {
+      const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
+      const int j0 = (int)(o0 & 0xFF), j1 = (int)(o1 & 0xFF);
+      float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
       uint32_t a[W32], b[W32];
       ld_row<W32>(rows + j0 * RS, a);
       ld_row<W32>(rows + j1 * RS, b);
@@ -928,16 +989,7 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
         fd1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
         fm1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
       }
-    }
-#pragma unroll
-    for (int q = 0; q < Q; q++) {
-      const float t0 = fmaf(fd0[q], c1, fmaf(fm0[q], c2, base[q]));
-      const float t1 = fmaf(fd1[q], c1, fmaf(fm1[q], c2, base[q]));
-      const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
-      mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
-      z[q] += e0 + e1;
-      ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
-      em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
+      sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
     }
   }
   if (i < n) {
