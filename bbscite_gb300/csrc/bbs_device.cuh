@@ -862,7 +862,8 @@ __device__ __forceinline__ uint32_t gene_increment(const SumCtx &sx, int j,
 
 // The float work of two nodes for the lane's cells (both count sources
 // share it, so the sums are the same whichever found the counts).
-template <int Q>
+// COUNTS: also the attachment-weighted counts (expected class counts).
+template <int Q, bool COUNTS>
 __device__ __forceinline__ void sum_pair(const float (&fd0)[Q],
                                          const float (&fm0)[Q],
                                          const float (&fd1)[Q],
@@ -877,8 +878,10 @@ __device__ __forceinline__ void sum_pair(const float (&fd0)[Q],
     const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
     mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
     z[q] += e0 + e1;
-    ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
-    em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
+    if constexpr (COUNTS) {
+      ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
+      em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
+    }
   }
 }
 
@@ -921,7 +924,20 @@ __device__ __forceinline__ void counts_to_float(const uint32_t (&k)[Q],
   }
 }
 
-template <int W32, int Q, bool INHERIT>
+// sum_pair on two nodes' packed counts.
+template <int Q, bool COUNTS>
+__device__ __forceinline__ void sum_counts(const uint32_t (&k0)[Q],
+                                           const uint32_t (&k1)[Q], float c1,
+                                           float c2, const float (&base)[Q],
+                                           float (&mx)[Q], float (&z)[Q],
+                                           float (&ed)[Q], float (&em)[Q]) {
+  float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
+  counts_to_float<Q>(k0, fd0, fm0);
+  counts_to_float<Q>(k1, fd1, fm1);
+  sum_pair<Q, COUNTS>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+}
+
+template <int W32, int Q, bool INHERIT, bool COUNTS>
 __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const Cells<W32, Q> &cb,
                                           const LogTable &L, int c0, int stride,
@@ -951,26 +967,26 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
   int i = 1;
   if constexpr (INHERIT) {
     // counts one pair ahead of the float work, which hides the table's
-    // load latency behind the previous pair's arithmetic
+    // load latency behind the previous pair's arithmetic; two pairs per
+    // iteration, alternating between two register sets
     if (i + 1 < n) {
-      uint32_t k0[Q], k1[Q];
-      inherit_pair<Q>(sx, i, c0, stride, lane, k0, k1);
+      uint32_t kA[Q], kB[Q], kA1[Q], kB1[Q];
+      inherit_pair<Q>(sx, i, c0, stride, lane, kA, kA1);
 #pragma unroll 1
-      for (; i + 1 < n; i += 2) {
-        uint32_t n0[Q], n1[Q];
-        const bool more = i + 3 < n;
-        if (more) inherit_pair<Q>(sx, i + 2, c0, stride, lane, n0, n1);
-        float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
-        counts_to_float<Q>(k0, fd0, fm0);
-        counts_to_float<Q>(k1, fd1, fm1);
-        sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
-        if (more) {
-#pragma unroll
-          for (int q = 0; q < Q; q++) {
-            k0[q] = n0[q];
-            k1[q] = n1[q];
-          }
-        }
+      for (; i + 5 < n; i += 4) {
+        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1);
+        sum_counts<Q, COUNTS>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1);
+        sum_counts<Q, COUNTS>(kB, kB1, c1, c2, base, mx, z, ed, em);
+      }
+      if (i + 3 < n) {
+        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1);
+        sum_counts<Q, COUNTS>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        sum_counts<Q, COUNTS>(kB, kB1, c1, c2, base, mx, z, ed, em);
+        i += 4;
+      } else {
+        sum_counts<Q, COUNTS>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        i += 2;
       }
     }
   } else {
@@ -989,7 +1005,7 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
         fd1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
         fm1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
       }
-      sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+      sum_pair<Q, COUNTS>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
     }
   }
   if (i < n) {
@@ -1021,8 +1037,10 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
       const float e = ex2_approx(t);
       mx[q] = fmaxf(mx[q], t);
       z[q] += e;
-      ed[q] = fmaf(e, fd[q], ed[q]);
-      em[q] = fmaf(e, fm[q], em[q]);
+      if constexpr (COUNTS) {
+        ed[q] = fmaf(e, fd[q], ed[q]);
+        em[q] = fmaf(e, fm[q], em[q]);
+      }
     }
   }
   bool bad[Q], any = false;
@@ -1061,8 +1079,10 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
         }
         const float e = ex2_approx(fmaf(fd, c1, fmaf(fm, c2, base[q])));
         z[q] += e;
-        ed[q] = fmaf(e, fd, ed[q]);
-        em[q] = fmaf(e, fm, em[q]);
+        if constexpr (COUNTS) {
+          ed[q] = fmaf(e, fd, ed[q]);
+          em[q] = fmaf(e, fm, em[q]);
+        }
       }
     }
   }
@@ -1070,14 +1090,16 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
   for (int q = 0; q < Q; q++) {
     const int c = c0 + stride * q + lane;
     if (c >= n_cells) continue;
-    const float inv = 1.0f / z[q];
-    const float Ed = ed[q] * inv, Em = em[q] * inv;
-    const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
     acc[0] += (long long)__float2int_rn((r[q] + logf(z[q])) * kScoreScale);
-    acc[1] += (long long)__float2int_rn((pd - Ed) * kFixScale);  // E[n00]
-    acc[2] += (long long)__float2int_rn(Ed * kFixScale);         // E[n01]
-    acc[3] += (long long)__float2int_rn((pm - Em) * kFixScale);  // E[n10]
-    acc[4] += (long long)__float2int_rn(Em * kFixScale);         // E[n11]
+    if constexpr (COUNTS) {
+      const float inv = 1.0f / z[q];
+      const float Ed = ed[q] * inv, Em = em[q] * inv;
+      const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
+      acc[1] += (long long)__float2int_rn((pd - Ed) * kFixScale);  // E[n00]
+      acc[2] += (long long)__float2int_rn(Ed * kFixScale);         // E[n01]
+      acc[3] += (long long)__float2int_rn((pm - Em) * kFixScale);  // E[n10]
+      acc[4] += (long long)__float2int_rn(Em * kFixScale);         // E[n11]
+    }
     acc[5] += (long long)__float2int_rn(fmaf(mx[q], kLn2, r[q]) * kScoreScale);
   }
 }
@@ -1086,38 +1108,48 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
 // warp-reduced), its terms added in the canonical order (sx.ord, built
 // here).  Inherited counts serve cells held in registers when sx brings the
 // parent vector, the count table and the increment table.
+// Returns whether acc[1..4] hold the expected counts: always but where
+// `counts` is false and the inherited counts served.
 template <int W32, int Q>
-__device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
+__device__ __forceinline__ bool sum_part(const uint32_t *rows, int n,
                                          const DatasetDev &ds,
                                          Cells<W32, Q> &cb, bool resident,
                                          const LogTable &L, int wpc, int wic,
                                          int lane, long long (&acc)[6],
-                                         const SumCtx &sx) {
+                                         const SumCtx &sx, bool counts) {
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = 0;
+  bool counts_done = true;
   canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
   if (resident) {
     bool inherit = false;
     if constexpr (W32 <= 4)
       inherit = sx.cnt != nullptr && sx.inc != nullptr && sx.par != nullptr;
     if (inherit) {
-      if constexpr (W32 <= 4)
-        sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
-                                ds.n_cells, acc, sx);
+      if constexpr (W32 <= 4) {
+        if (counts)
+          sum_cells<W32, Q, true, true>(rows, n, cb, L, 32 * wic, 32 * wpc,
+                                        lane, ds.n_cells, acc, sx);
+        else
+          sum_cells<W32, Q, true, false>(rows, n, cb, L, 32 * wic, 32 * wpc,
+                                         lane, ds.n_cells, acc, sx);
+      }
+      counts_done = counts;
     } else {
-      sum_cells<W32, Q, false>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
-                               ds.n_cells, acc, sx);
+      sum_cells<W32, Q, false, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
+                                     ds.n_cells, acc, sx);
     }
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      sum_cells<W32, Q, false>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc, lane,
-                               ds.n_cells, acc, sx);
+      sum_cells<W32, Q, false, true>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc,
+                                     lane, ds.n_cells, acc, sx);
     }
   }
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = warp_sum_ll(acc[i]);
+  return counts_done;
 }
 
 // Class totals (n00, n01, n10, n11) from the sums.
