@@ -862,8 +862,7 @@ __device__ __forceinline__ uint32_t gene_increment(const SumCtx &sx, int j,
 
 // The float work of two nodes for the lane's cells (both count sources
 // share it, so the sums are the same whichever found the counts).
-// COUNTS: also the attachment-weighted counts (expected class counts).
-template <int Q, bool COUNTS>
+template <int Q>
 __device__ __forceinline__ void sum_pair(const float (&fd0)[Q],
                                          const float (&fm0)[Q],
                                          const float (&fd1)[Q],
@@ -878,10 +877,8 @@ __device__ __forceinline__ void sum_pair(const float (&fd0)[Q],
     const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
     mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
     z[q] += e0 + e1;
-    if constexpr (COUNTS) {
-      ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
-      em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
-    }
+    ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
+    em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
   }
 }
 
@@ -925,7 +922,7 @@ __device__ __forceinline__ void counts_to_float(const uint32_t (&k)[Q],
 }
 
 // sum_pair on two nodes' packed counts.
-template <int Q, bool COUNTS>
+template <int Q>
 __device__ __forceinline__ void sum_counts(const uint32_t (&k0)[Q],
                                            const uint32_t (&k1)[Q], float c1,
                                            float c2, const float (&base)[Q],
@@ -934,10 +931,61 @@ __device__ __forceinline__ void sum_counts(const uint32_t (&k0)[Q],
   float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
   counts_to_float<Q>(k0, fd0, fm0);
   counts_to_float<Q>(k1, fd1, fm1);
-  sum_pair<Q, COUNTS>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+  sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
 }
 
-template <int W32, int Q, bool INHERIT, bool COUNTS>
+// Q floats, passed and returned by value.
+template <int Q>
+struct QF {
+  float v[Q];
+};
+
+template <int Q>
+struct Resum {
+  QF<Q> z, ed, em;
+};
+
+// The second pass of the cells in `bad` (bit q: cell slot q), each against
+// its own maximum (base already shifted), one node at a time in the
+// canonical order.  Rarely taken, so kept out of line: the node loop's code
+// stays small, and the cells come by value.
+template <int W32, int Q, bool INHERIT>
+__device__ __noinline__ Resum<Q> resum_cells(const uint32_t *rows, int n,
+                                             const Cells<W32, Q> cb,
+                                             const SumCtx sx, int lane,
+                                             float c1, float c2,
+                                             const QF<Q> base, unsigned bad) {
+  constexpr int RS = rs_of_w32(W32);
+  Resum<Q> o;
+#pragma unroll
+  for (int q = 0; q < Q; q++) o.z.v[q] = o.ed.v[q] = o.em.v[q] = 0.0f;
+#pragma unroll 1
+  for (int i2 = 0; i2 < n; i2++) {
+    const int j = (int)(sx.ord[i2] & 0xFF);
+    uint32_t a[W32];
+    if constexpr (!INHERIT) ld_row<W32>(rows + j * RS, a);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      if (!((bad >> q) & 1u)) continue;
+      float fd, fm;
+      if constexpr (INHERIT) {
+        const uint32_t k = sx.cnt[(j * Q + q) * 32 + lane];
+        fd = __int_as_float(0x4B000000 | (k & 0xFFu)) - 8388608.0f;
+        fm = __int_as_float(0x4B000000 | (k >> 8)) - 8388608.0f;
+      } else {
+        fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
+        fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
+      }
+      const float e = ex2_approx(fmaf(fd, c1, fmaf(fm, c2, base.v[q])));
+      o.z.v[q] += e;
+      o.ed.v[q] = fmaf(e, fd, o.ed.v[q]);
+      o.em.v[q] = fmaf(e, fm, o.em.v[q]);
+    }
+  }
+  return o;
+}
+
+template <int W32, int Q, bool INHERIT>
 __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const Cells<W32, Q> &cb,
                                           const LogTable &L, int c0, int stride,
@@ -975,17 +1023,17 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
 #pragma unroll 1
       for (; i + 5 < n; i += 4) {
         inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1);
-        sum_counts<Q, COUNTS>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
         inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1);
-        sum_counts<Q, COUNTS>(kB, kB1, c1, c2, base, mx, z, ed, em);
+        sum_counts<Q>(kB, kB1, c1, c2, base, mx, z, ed, em);
       }
       if (i + 3 < n) {
         inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1);
-        sum_counts<Q, COUNTS>(kA, kA1, c1, c2, base, mx, z, ed, em);
-        sum_counts<Q, COUNTS>(kB, kB1, c1, c2, base, mx, z, ed, em);
+        sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        sum_counts<Q>(kB, kB1, c1, c2, base, mx, z, ed, em);
         i += 4;
       } else {
-        sum_counts<Q, COUNTS>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
         i += 2;
       }
     }
@@ -1005,7 +1053,7 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
         fd1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
         fm1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
       }
-      sum_pair<Q, COUNTS>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+      sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
     }
   }
   if (i < n) {
@@ -1037,10 +1085,8 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
       const float e = ex2_approx(t);
       mx[q] = fmaxf(mx[q], t);
       z[q] += e;
-      if constexpr (COUNTS) {
-        ed[q] = fmaf(e, fd[q], ed[q]);
-        em[q] = fmaf(e, fm[q], em[q]);
-      }
+      ed[q] = fmaf(e, fd[q], ed[q]);
+      em[q] = fmaf(e, fm[q], em[q]);
     }
   }
   bool bad[Q], any = false;
@@ -1052,54 +1098,40 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
   if (__any_sync(BBS_FULL_MASK, any)) {
     // cells summed once more against their maximum, one node at a time in
     // the same order
+    QF<Q> b2;
+    unsigned badm = 0;
 #pragma unroll
-    for (int q = 0; q < Q; q++)
+    for (int q = 0; q < Q; q++) {
       if (bad[q]) {
         r[q] = fmaf(mx[q], kLn2, r[q]);
         base[q] -= mx[q];
         mx[q] = 0.0f;
-        z[q] = ed[q] = em[q] = 0.0f;
+        badm |= 1u << q;
       }
-#pragma unroll 1
-    for (int i2 = 0; i2 < n; i2++) {
-      const int j = (int)(sx.ord[i2] & 0xFF);
-      uint32_t a[W32];
-      if constexpr (!INHERIT) ld_row<W32>(rows + j * RS, a);
-#pragma unroll
-      for (int q = 0; q < Q; q++) {
-        if (!bad[q]) continue;
-        float fd, fm;
-        if constexpr (INHERIT) {
-          const uint32_t k = sx.cnt[(j * Q + q) * 32 + lane];
-          fd = __int_as_float(0x4B000000 | (k & 0xFFu)) - 8388608.0f;
-          fm = __int_as_float(0x4B000000 | (k >> 8)) - 8388608.0f;
-        } else {
-          fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
-          fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
-        }
-        const float e = ex2_approx(fmaf(fd, c1, fmaf(fm, c2, base[q])));
-        z[q] += e;
-        if constexpr (COUNTS) {
-          ed[q] = fmaf(e, fd, ed[q]);
-          em[q] = fmaf(e, fm, em[q]);
-        }
-      }
+      b2.v[q] = base[q];
     }
+    const Resum<Q> o = resum_cells<W32, Q, INHERIT>(rows, n, cb, sx, lane,
+                                                           c1, c2, b2, badm);
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+      if (bad[q]) {
+        z[q] = o.z.v[q];
+        ed[q] = o.ed.v[q];
+        em[q] = o.em.v[q];
+      }
   }
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     const int c = c0 + stride * q + lane;
     if (c >= n_cells) continue;
+    const float inv = 1.0f / z[q];
+    const float Ed = ed[q] * inv, Em = em[q] * inv;
+    const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
     acc[0] += (long long)__float2int_rn((r[q] + logf(z[q])) * kScoreScale);
-    if constexpr (COUNTS) {
-      const float inv = 1.0f / z[q];
-      const float Ed = ed[q] * inv, Em = em[q] * inv;
-      const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
-      acc[1] += (long long)__float2int_rn((pd - Ed) * kFixScale);  // E[n00]
-      acc[2] += (long long)__float2int_rn(Ed * kFixScale);         // E[n01]
-      acc[3] += (long long)__float2int_rn((pm - Em) * kFixScale);  // E[n10]
-      acc[4] += (long long)__float2int_rn(Em * kFixScale);         // E[n11]
-    }
+    acc[1] += (long long)__float2int_rn((pd - Ed) * kFixScale);  // E[n00]
+    acc[2] += (long long)__float2int_rn(Ed * kFixScale);         // E[n01]
+    acc[3] += (long long)__float2int_rn((pm - Em) * kFixScale);  // E[n10]
+    acc[4] += (long long)__float2int_rn(Em * kFixScale);         // E[n11]
     acc[5] += (long long)__float2int_rn(fmaf(mx[q], kLn2, r[q]) * kScoreScale);
   }
 }
@@ -1108,48 +1140,38 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
 // warp-reduced), its terms added in the canonical order (sx.ord, built
 // here).  Inherited counts serve cells held in registers when sx brings the
 // parent vector, the count table and the increment table.
-// Returns whether acc[1..4] hold the expected counts: always but where
-// `counts` is false and the inherited counts served.
 template <int W32, int Q>
-__device__ __forceinline__ bool sum_part(const uint32_t *rows, int n,
+__device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
                                          const DatasetDev &ds,
                                          Cells<W32, Q> &cb, bool resident,
                                          const LogTable &L, int wpc, int wic,
                                          int lane, long long (&acc)[6],
-                                         const SumCtx &sx, bool counts) {
+                                         const SumCtx &sx) {
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = 0;
-  bool counts_done = true;
   canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
   if (resident) {
     bool inherit = false;
     if constexpr (W32 <= 4)
       inherit = sx.cnt != nullptr && sx.inc != nullptr && sx.par != nullptr;
     if (inherit) {
-      if constexpr (W32 <= 4) {
-        if (counts)
-          sum_cells<W32, Q, true, true>(rows, n, cb, L, 32 * wic, 32 * wpc,
-                                        lane, ds.n_cells, acc, sx);
-        else
-          sum_cells<W32, Q, true, false>(rows, n, cb, L, 32 * wic, 32 * wpc,
-                                         lane, ds.n_cells, acc, sx);
-      }
-      counts_done = counts;
+      if constexpr (W32 <= 4)
+        sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
+                                ds.n_cells, acc, sx);
     } else {
-      sum_cells<W32, Q, false, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
-                                     ds.n_cells, acc, sx);
+      sum_cells<W32, Q, false>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
+                               ds.n_cells, acc, sx);
     }
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      sum_cells<W32, Q, false, true>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc,
-                                     lane, ds.n_cells, acc, sx);
+      sum_cells<W32, Q, false>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc, lane,
+                               ds.n_cells, acc, sx);
     }
   }
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = warp_sum_ll(acc[i]);
-  return counts_done;
 }
 
 // Class totals (n00, n01, n10, n11) from the sums.

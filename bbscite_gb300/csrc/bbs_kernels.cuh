@@ -68,12 +68,6 @@ __host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
   return sum && w32 <= 4 ? align16(2 * n * 32 * q * wpc) : 0;
 }
 
-// sx for the tree whose parent vector is par.
-__device__ __forceinline__ SumCtx sx_at(SumCtx sx, const uint8_t *par) {
-  sx.par = par;
-  return sx;
-}
-
 // The sum-score pieces of a slot: parent vectors and warp wic's scratch.
 struct SlotSum {
   uint8_t *par0, *par1;
@@ -115,8 +109,7 @@ __device__ __forceinline__ void build_increments(uint16_t *table, int stride,
 }
 
 // Evaluates a tree for the whole chain (all wpc warps): returns the score
-// S = data term + prior and the (exact or expected) class counts e[4]
-// (for the sum score only where `counts` comes back true);
+// S = data term + prior and the (exact or expected) class counts e[4];
 // sk, sm are the class sums of the max score and smax the max score itself
 // (S for the max score; for the sum score, sum_c max_j s_cj + prior).
 template <int W32, int Q, bool SUM>
@@ -126,7 +119,7 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
                                           const LogTable &L, float prior,
                                           int wpc, int wic, int lane,
                                           int *part, int parity,
-                                          const SumCtx &sx, bool &counts,
+                                          const SumCtx &sx,
                                           float (&e)[4], int &sk, int &sm,
                                           float &smax) {
   if constexpr (!SUM) {
@@ -155,9 +148,7 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
     return smax;
   } else {
     long long acc[6];
-    // in: expected counts wanted; out: expected counts in e
-    counts = sum_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane,
-                              acc, sx, counts);
+    sum_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, acc, sx);
     if (wpc > 1) {
       long long *pp = reinterpret_cast<long long *>(part) + parity * 6 * wpc;
       if (lane == 0)
@@ -208,11 +199,6 @@ __device__ __forceinline__ void run_chain(
   float alpha = st.alpha, beta = st.beta, score = st.score, prior = st.prior;
   LogTable L{st.l00, st.l10, st.l01, st.l11};
   float ec[4] = {st.ec[0], st.ec[1], st.ec[2], st.ec[3]};
-  // The sum score's expected counts feed only the learned error moves'
-  // geometry at the current state: tree proposals skip them, and they are
-  // found again (the same evaluation of the same tree) when an error move
-  // or the end of the launch needs them.
-  bool ec_valid = true;
   int csk = st.sk, csm = st.sm;
   bool has_best = st.has_best != 0;
   float best_score = st.best_score, best_alpha = st.best_alpha,
@@ -275,19 +261,6 @@ __device__ __forceinline__ void run_chain(
     } else {
       // (preconditioned) random walk or Langevin step in logit space, with
       // the geometry of the current state from its class counts
-      if (!ec_valid) {
-        float e2[4], s2;
-        int k2, m2;
-        bool want = true;
-        // this step's parity: the step's barrier below separates these
-        // partial sums from the proposal's
-        evaluate<W32, Q, SUM>(cur, n, ds, cb, resident, L, prior, wpc, wic,
-                              lane, part, i & 1, sx_at(sx, cpar), want, e2, k2,
-                              m2, s2);
-#pragma unroll
-        for (int k = 0; k < 4; k++) ec[k] = e2[k];
-        ec_valid = true;
-      }
       geo = error_geometry(ds, alpha, beta, md.gamma, ec);
       float z0, z1;
       error_normals(raw, z0, z1);
@@ -319,12 +292,9 @@ __device__ __forceinline__ void run_chain(
 #endif
     float e[4], psmax;
     int sk, sm;
-    // expected counts are needed of learned error-move proposals only
-    bool counts = err_move && learn;
     const float pscore = evaluate<W32, Q, SUM>(scored, n, ds, cb, resident, PL,
                                                pprior, wpc, wic, lane, part,
-                                               i & 1, sx, counts, e, sk, sm,
-                                               psmax);
+                                               i & 1, sx, e, sk, sm, psmax);
     bool accept;
     if (err_move && learn) {
       const ErrorGeom pgeo = error_geometry(ds, palpha, pbeta, md.gamma, e);
@@ -413,21 +383,10 @@ __device__ __forceinline__ void run_chain(
       L = PL;
 #pragma unroll
       for (int k = 0; k < 4; k++) ec[k] = e[k];
-      ec_valid = !SUM || counts;
       csk = sk;
       csm = sm;
     }
     __syncwarp();
-  }
-  if (!ec_valid) {  // the saved state carries its expected counts
-    float e2[4], s2;
-    int k2, m2;
-    bool want = true;
-    // the parity after the last step's
-    evaluate<W32, Q, SUM>(cur, n, ds, cb, resident, L, prior, wpc, wic, lane,
-                          part, i & 1, sx_at(sx, cpar), want, e2, k2, m2, s2);
-#pragma unroll
-    for (int k = 0; k < 4; k++) ec[k] = e2[k];
   }
   copy_rows_part<W32>(cur, g, n, wpc, wic, lane);
   if (wic == 0 && lane == 0) {
@@ -648,10 +607,8 @@ __global__ void __launch_bounds__(128) init_kernel(const InitArgs a) {
   Cells<W32, Q> cb;
   float e[4], smax;
   int sk, sm;
-  bool counts = true;
   const float S = evaluate<W32, Q, SUM>(rows, n, ds, cb, false, L, prior, 1, 0,
-                                        lane, nullptr, 0, sx, counts, e, sk, sm,
-                                        smax);
+                                        lane, nullptr, 0, sx, e, sk, sm, smax);
   if (lane == 0) {
     ChainState o;
     o.alpha = alpha;
