@@ -446,9 +446,10 @@ __device__ __forceinline__ float pair_score(int d, int m, float pdb,
 }
 
 // 64-bit hash of a tree's ancestor rows, the same in every lane: a mix of
-// each word with its position, summed and xor-ed over the warp.
+// each word with its position, summed and xor-ed over the warp.  Only
+// co-optimal tree lists use it, so it is kept out of line.
 template <int W32>
-__device__ __forceinline__ uint64_t tree_hash(const uint32_t *rows, int n,
+__device__ __noinline__ uint64_t tree_hash(const uint32_t *rows, int n,
                                               int lane) {
   constexpr int RS = rs_of_w32(W32);
   uint32_t h0 = 0, h1 = 0;
@@ -753,8 +754,9 @@ __device__ __forceinline__ void canonical_order(const uint32_t *rows, int n,
 
 // The parent vector of the tree with ancestor rows `rows`: each node's
 // deepest proper ancestor (the root is its own parent).  depth_tmp: n ints.
+// Once per launch, so out of line.
 template <int W32>
-__device__ __forceinline__ void derive_parents(const uint32_t *rows, int n,
+__device__ __noinline__ void derive_parents(const uint32_t *rows, int n,
                                                uint8_t *par, int *depth_tmp,
                                                int lane) {
   constexpr int RS = rs_of_w32(W32);
@@ -1140,6 +1142,29 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
 // warp-reduced), its terms added in the canonical order (sx.ord, built
 // here).  Inherited counts serve cells held in registers when sx brings the
 // parent vector, the count table and the increment table.
+// The masked-popcount node loop for rows of up to four words, out of line:
+// there it serves only streamed cells and mixed launch groups, and keeping
+// one copy of it outside the chain kernels leaves the inherited-count loop
+// and the step code small.  Wider rows have no other loop and keep it
+// inline.
+struct Acc6 {
+  long long v[6];
+};
+
+template <int W32, int Q>
+__device__ __noinline__ Acc6 sum_cells_popc(const uint32_t *rows, int n,
+                                            const Cells<W32, Q> cb,
+                                            const LogTable L, int c0,
+                                            int stride, int lane, int n_cells,
+                                            const SumCtx sx) {
+  long long acc[6] = {0, 0, 0, 0, 0, 0};
+  sum_cells<W32, Q, false>(rows, n, cb, L, c0, stride, lane, n_cells, acc, sx);
+  Acc6 o;
+#pragma unroll
+  for (int i = 0; i < 6; i++) o.v[i] = acc[i];
+  return o;
+}
+
 template <int W32, int Q>
 __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
                                          const DatasetDev &ds,
@@ -1159,15 +1184,29 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
         sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
                                 ds.n_cells, acc, sx);
     } else {
-      sum_cells<W32, Q, false>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
-                               ds.n_cells, acc, sx);
+      if constexpr (W32 <= 4) {
+        const Acc6 o = sum_cells_popc<W32, Q>(rows, n, cb, L, 32 * wic,
+                                              32 * wpc, lane, ds.n_cells, sx);
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc[k] += o.v[k];
+      } else {
+        sum_cells<W32, Q, false>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
+                                 ds.n_cells, acc, sx);
+      }
     }
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      sum_cells<W32, Q, false>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc, lane,
-                               ds.n_cells, acc, sx);
+      if constexpr (W32 <= 4) {
+        const Acc6 o = sum_cells_popc<W32, Q>(rows, n, cb, L, c0 + 32 * wic,
+                                              32 * wpc, lane, ds.n_cells, sx);
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc[k] += o.v[k];
+      } else {
+        sum_cells<W32, Q, false>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc,
+                                 lane, ds.n_cells, acc, sx);
+      }
     }
   }
 #pragma unroll
