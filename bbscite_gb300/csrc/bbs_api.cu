@@ -840,7 +840,9 @@ void default_launch(bbs_ctx *c) {
     c->wpc = 4;
     c->q = qmax;
   }
-  c->cpb = c->wpc == 1 ? (c->n_chains >= (uint32_t)c->n_sms * 16 ? 4 : 1) : 1;
+  // four one-warp chains per block share the block's increment table, and
+  // two such blocks fit an SM's shared memory
+  c->cpb = c->wpc == 1 ? 4 : 1;
 }
 
 size_t tree_words(const bbs_ctx *c, uint32_t n_trees) {
@@ -1926,7 +1928,7 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.cancel = nullptr;
     a.status = b->d_status;
     a.max_nodes = grp.max_nodes;
-    a.table_ds = b->sum ? grp.only_ds : -1;
+    a.table_ds = grp.only_ds;
     const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;  // 1, 2 above 128 nodes
     const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");

@@ -429,11 +429,9 @@ __device__ __forceinline__ int masked_popc(const uint32_t (&X)[W32],
 // n01 = d, n11 = m, n00 = popc(D) - d, n10 = popc(M) - m.  Biased floats
 // 2^23 + i (bit pattern 0x4B000000 + i) make every difference exact:
 //   pdb = 2^23 + popc(D),  pmb = 2^23 + popc(M).
-__device__ __forceinline__ float pair_score(int d, int m, float pdb,
-                                            float pmb, float l00, float l01,
-                                            float l10, float l11) {
-  const float db = __int_as_float(0x4B000000 + d);
-  const float mb = __int_as_float(0x4B000000 + m);
+__device__ __forceinline__ float pair_score_b(float db, float mb, float pdb,
+                                              float pmb, float l00, float l01,
+                                              float l10, float l11) {
   const float f01 = __fsub_rn(db, 8388608.0f);
   const float f11 = __fsub_rn(mb, 8388608.0f);
   const float f00 = __fsub_rn(pdb, db);
@@ -443,6 +441,15 @@ __device__ __forceinline__ float pair_score(int d, int m, float pdb,
   s = __fadd_rn(s, __fmul_rn(f10, l10));
   s = __fadd_rn(s, __fmul_rn(f11, l11));
   return s;
+}
+
+// The same from the integer counts.
+__device__ __forceinline__ float pair_score(int d, int m, float pdb,
+                                            float pmb, float l00, float l01,
+                                            float l10, float l11) {
+  return pair_score_b(__int_as_float(0x4B000000 + d),
+                      __int_as_float(0x4B000000 + m), pdb, pmb, l00, l01, l10,
+                      l11);
 }
 
 // 64-bit hash of a tree's ancestor rows, the same in every lane: a mix of
@@ -590,32 +597,6 @@ __device__ __forceinline__ void counts_at(const uint32_t *rows,
 struct LogTable {
   float l00, l10, l01, l11;
 };
-
-// This warp's part of the class sums over its cells (max score).  Cells
-// are split over the `wpc` warps of a chain: cell = c0 + 32*wpc*q +
-// 32*wic + lane.  With `resident`, cb already holds the warp's cells.
-template <int W32, int Q>
-__device__ __forceinline__ void score_part(const uint32_t *rows, int n,
-                                           const DatasetDev &ds,
-                                           Cells<W32, Q> &cb, bool resident,
-                                           const LogTable &L, int wpc,
-                                           int wic, int lane, int &sk,
-                                           int &sm) {
-  int k = 0, m = 0, bj[Q];
-  if (resident) {
-    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
-    counts_at<W32, Q>(rows, cb, bj, k, m);
-  } else {
-    const int span = 32 * wpc * Q;
-    for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
-      load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
-      counts_at<W32, Q>(rows, cb, bj, k, m);
-    }
-  }
-  sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);
-  sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
-}
 
 // Sum-over-attachments pass with its adjoint, for the lane's Q cells.
 // Per cell the scores s_j are summed as exp(s_j - r) against a reference r
@@ -892,10 +873,12 @@ template <int Q>
 __device__ __forceinline__ void inherit_pair(const SumCtx &sx, int i, int c0,
                                              int stride, int lane,
                                              uint32_t (&k0)[Q],
-                                             uint32_t (&k1)[Q]) {
+                                             uint32_t (&k1)[Q], int &j0,
+                                             int &j1) {
   const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
-  const int j0 = (int)(o0 & 0xFF), p0 = (int)(o0 >> 8);
-  const int j1 = (int)(o1 & 0xFF), p1 = (int)(o1 >> 8);
+  j0 = (int)(o0 & 0xFF);
+  j1 = (int)(o1 & 0xFF);
+  const int p0 = (int)(o0 >> 8), p1 = (int)(o1 >> 8);
   uint32_t a0[Q], a1[Q], g0[Q], g1[Q];
 #pragma unroll
   for (int q = 0; q < Q; q++) {
@@ -1021,16 +1004,17 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     // iteration, alternating between two register sets
     if (i + 1 < n) {
       uint32_t kA[Q], kB[Q], kA1[Q], kB1[Q];
-      inherit_pair<Q>(sx, i, c0, stride, lane, kA, kA1);
+      int jA0, jA1, jB0, jB1;  // node numbers (the max score uses them)
+      inherit_pair<Q>(sx, i, c0, stride, lane, kA, kA1, jA0, jA1);
 #pragma unroll 1
       for (; i + 5 < n; i += 4) {
-        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1);
+        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
         sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
-        inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1);
+        inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1, jA0, jA1);
         sum_counts<Q>(kB, kB1, c1, c2, base, mx, z, ed, em);
       }
       if (i + 3 < n) {
-        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1);
+        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
         sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
         sum_counts<Q>(kB, kB1, c1, c2, base, mx, z, ed, em);
         i += 4;
@@ -1211,6 +1195,131 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
   }
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = warp_sum_ll(acc[i]);
+}
+
+// Max score with inherited counts (rows of up to four words, cells in
+// registers): the nodes in the canonical order with their counts found one
+// pair ahead as for the sum score, each node's score in the reference's
+// order, and the first maximum in node-index order -- an equal score at a
+// lower index wins, which is what std::max over the nodes in index order
+// keeps (src/TreeScorer.hpp:187-193) -- so the chosen nodes, and the class
+// counts at them, are those of best_nodes.
+template <int Q>
+__device__ __forceinline__ void max_update(const uint32_t (&k)[Q], int j,
+                                           const float (&pdb)[Q],
+                                           const float (&pmb)[Q],
+                                           const LogTable &L,
+                                           float (&best)[Q], int (&bj)[Q]) {
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const float s = pair_score_b(__int_as_float(0x4B000000 | (k[q] & 0xFFu)),
+                                 __int_as_float(0x4B000000 | (k[q] >> 8)),
+                                 pdb[q], pmb[q], L.l00, L.l01, L.l10, L.l11);
+    const bool up = s > best[q] || (s == best[q] && j < bj[q]);
+    best[q] = up ? s : best[q];
+    bj[q] = up ? j : bj[q];
+  }
+}
+
+template <int W32, int Q>
+__device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb,
+                                                  const LogTable &L, int c0,
+                                                  int stride, int lane,
+                                                  const SumCtx &sx, int &k,
+                                                  int &m) {
+  float best[Q];
+  int bj[Q];
+  {
+    const int root = (int)(sx.ord[0] & 0xFF);
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      sx.cnt[(root * Q + q) * 32 + lane] = 0;
+      best[q] = pair_score(0, 0, cb.pdb[q], cb.pmb[q], L.l00, L.l01, L.l10,
+                           L.l11);
+      bj[q] = root;
+    }
+  }
+  int i = 1;
+  if (i + 1 < n) {
+    uint32_t kA[Q], kB[Q], kA1[Q], kB1[Q];
+    int jA0, jA1, jB0, jB1;
+    inherit_pair<Q>(sx, i, c0, stride, lane, kA, kA1, jA0, jA1);
+#pragma unroll 1
+    for (; i + 5 < n; i += 4) {
+      inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
+      max_update<Q>(kA, jA0, cb.pdb, cb.pmb, L, best, bj);
+      max_update<Q>(kA1, jA1, cb.pdb, cb.pmb, L, best, bj);
+      inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1, jA0, jA1);
+      max_update<Q>(kB, jB0, cb.pdb, cb.pmb, L, best, bj);
+      max_update<Q>(kB1, jB1, cb.pdb, cb.pmb, L, best, bj);
+    }
+    if (i + 3 < n) {
+      inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
+      max_update<Q>(kA, jA0, cb.pdb, cb.pmb, L, best, bj);
+      max_update<Q>(kA1, jA1, cb.pdb, cb.pmb, L, best, bj);
+      max_update<Q>(kB, jB0, cb.pdb, cb.pmb, L, best, bj);
+      max_update<Q>(kB1, jB1, cb.pdb, cb.pmb, L, best, bj);
+      i += 4;
+    } else {
+      max_update<Q>(kA, jA0, cb.pdb, cb.pmb, L, best, bj);
+      max_update<Q>(kA1, jA1, cb.pdb, cb.pmb, L, best, bj);
+      i += 2;
+    }
+  }
+  if (i < n) {
+    const uint32_t o = sx.ord[i];
+    const int j = (int)(o & 0xFF), p = (int)(o >> 8);
+    uint32_t kk[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      kk[q] = (uint32_t)sx.cnt[(p * Q + q) * 32 + lane] +
+              gene_increment(sx, j, c0 + stride * q + lane);
+      sx.cnt[(j * Q + q) * 32 + lane] = (uint16_t)kk[q];
+    }
+    max_update<Q>(kk, j, cb.pdb, cb.pmb, L, best, bj);
+  }
+  // the counts at the chosen nodes: k = popc(K & A) = d + m
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const uint32_t c = sx.cnt[(bj[q] * Q + q) * 32 + lane];
+    k += (int)(c & 0xFFu) + (int)(c >> 8);
+    m += (int)(c >> 8);
+  }
+}
+
+// This warp's part of the class sums over its cells (max score).  Cells
+// are split over the `wpc` warps of a chain: cell = c0 + 32*wpc*q +
+// 32*wic + lane.  With `resident`, cb already holds the warp's cells.
+template <int W32, int Q>
+__device__ __forceinline__ void score_part(const uint32_t *rows, int n,
+                                           const DatasetDev &ds,
+                                           Cells<W32, Q> &cb, bool resident,
+                                           const LogTable &L, int wpc,
+                                           int wic, int lane, int &sk,
+                                           int &sm, const SumCtx &sx) {
+  int k = 0, m = 0, bj[Q];
+  bool inherit = false;
+  if constexpr (W32 <= 4)
+    inherit = resident && sx.cnt != nullptr && sx.inc != nullptr &&
+              sx.par != nullptr;
+  if (inherit) {
+    if constexpr (W32 <= 4) {
+      canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
+      max_cells_inherit<W32, Q>(n, cb, L, 32 * wic, 32 * wpc, lane, sx, k, m);
+    }
+  } else if (resident) {
+    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
+    counts_at<W32, Q>(rows, cb, bj, k, m);
+  } else {
+    const int span = 32 * wpc * Q;
+    for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
+      load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
+      best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
+      counts_at<W32, Q>(rows, cb, bj, k, m);
+    }
+  }
+  sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);
+  sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
 }
 
 // Class totals (n00, n01, n10, n11) from the sums.

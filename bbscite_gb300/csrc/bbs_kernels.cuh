@@ -61,8 +61,14 @@ __host__ __device__ inline int slot_bytes(int n, int rs, int wpc, bool sum,
   return b;
 }
 
-// After the slots: the block's table of per-gene increments (sum score,
-// rows of up to four words) for its 32 * q * wpc resident cell slots.
+// Kernels with the node-order scratch: every sum-score kernel (its order
+// is canonical) and every kernel with rows of up to four words (inherited
+// counts, max or sum score).
+template <int W32, bool SUM>
+inline constexpr bool kScratch = SUM || W32 <= 4;
+
+// After the slots: the block's table of per-gene increments (rows of up to
+// four words) for its 32 * q * wpc resident cell slots.
 __host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
                                            bool sum) {
   return sum && w32 <= 4 ? align16(2 * n * 32 * q * wpc) : 0;
@@ -124,7 +130,7 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
                                           float &smax) {
   if constexpr (!SUM) {
     int a, b;
-    score_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, a, b);
+    score_part<W32, Q>(rows, n, ds, cb, resident, L, wpc, wic, lane, a, b, sx);
     if (wpc > 1) {
       int *pp = part + parity * 12 * wpc;
       if (lane == 0) {
@@ -184,15 +190,22 @@ __device__ __forceinline__ void run_chain(
   copy_rows_part<W32>(g, buf0, n, wpc, wic, lane);
   if (multi) __syncthreads(); else __syncwarp();
   uint32_t *cur = buf0, *prop = buf1;
-  // Sum score with inherited counts: the parent vectors of the current tree
-  // and of the proposal follow the rows.
+  // Inherited counts (rows of up to four words): the parent vectors of the
+  // current tree and of the proposal follow the rows.  A parent vector is
+  // used only after it has been checked against its rows: a realised move
+  // whose k-th (non)descendant fell back to node 0 (the reference's rule
+  // when floor(u * count) reaches the count) changes the rows in a way the
+  // parent-vector form does not follow, and may leave rows that are no tree.
+  // Such trees are scored with masked popcounts, which take any rows.
   uint8_t *cpar = nullptr, *ppar = nullptr;
-  if constexpr (SUM && W32 <= 4) {
+  bool cur_par_ok = false;  // cpar describes cur
+  if constexpr (W32 <= 4) {
     if (ss.sx.inc != nullptr && resident) {
       cpar = ss.par0;
       ppar = ss.par1;
       if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
       if (multi) __syncthreads(); else __syncwarp();
+      cur_par_ok = parents_match_rows<W32>(cur, n, cpar, lane);
     }
   }
   SumCtx sx = ss.sx;
@@ -244,7 +257,7 @@ __device__ __forceinline__ void run_chain(
       }
       build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
                           lane);
-      if (cpar != nullptr && wic == 0)
+      if (cur_par_ok && wic == 0)
         propose_parents(cpar, ppar, n, R.p, R.related, lane);
       scored = prop;
       // src/Application.hpp:443-450
@@ -278,18 +291,16 @@ __device__ __forceinline__ void run_chain(
       beta_terms_f(ds, pbeta, PL.l01, PL.l11, pprior);
     }
     if (multi) __syncthreads(); else __syncwarp();
-    sx.par = cpar == nullptr ? nullptr : (scored == cur ? cpar : ppar);
-#ifdef BBS_CHECKED
-    if constexpr (SUM && W32 <= 4) {
-      // the proposal's parent vector against its rows (value: move type)
-      if (cpar != nullptr && scored != cur &&
-          !device_check(parents_match_rows<W32>(scored, n, ppar, lane), status,
-                        kCheckParent, (uint32_t)raw.move_type, 4u)) {
-        cancelled = true;  // the chain stops where it is
-        break;
-      }
+    // the evaluated tree's parent vector, used only where it checks out
+    // against the rows (so the counts never depend on how it was found)
+    bool par_ok = false;
+    if constexpr (W32 <= 4) {
+      if (cpar != nullptr && cur_par_ok)
+        par_ok = parents_match_rows<W32>(scored, n, scored == cur ? cpar : ppar,
+                                         lane);
     }
-#endif
+    sx.par = par_ok ? (scored == cur ? cpar : ppar) : nullptr;
+    const bool prop_par_ok = par_ok && scored != cur;
     float e[4], psmax;
     int sk, sm;
     const float pscore = evaluate<W32, Q, SUM>(scored, n, ds, cb, resident, PL,
@@ -375,6 +386,16 @@ __device__ __forceinline__ void run_chain(
         uint8_t *tp = cpar;
         cpar = ppar;
         ppar = tp;
+        if constexpr (W32 <= 4) {
+          cur_par_ok = prop_par_ok;
+          if (cpar != nullptr && !cur_par_ok) {
+            // the new tree's own parent vector, where its rows are a tree
+            if (multi) __syncthreads(); else __syncwarp();
+            if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
+            if (multi) __syncthreads(); else __syncwarp();
+            cur_par_ok = parents_match_rows<W32>(cur, n, cpar, lane);
+          }
+        }
       }
       alpha = palpha;
       beta = pbeta;
@@ -442,7 +463,7 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   const int cpb = wpb / wpc;
   const int slot = wib / wpc, wic = wib - slot * wpc;
   const int n = a.ds.n_nodes;
-  const int sb = slot_bytes(n, RS, wpc, SUM, W32, Q);
+  const int sb = slot_bytes(n, RS, wpc, kScratch<W32, SUM>, W32, Q);
   uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)slot * sb;
   uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   uint32_t *buf1 = buf0 + n * RS;
@@ -452,7 +473,7 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   Cells<W32, Q> cb;
   if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
   SlotSum ss{};
-  if constexpr (SUM) {
+  if constexpr (kScratch<W32, SUM>) {
     ss = slot_sum(slot_base, n, RS, wpc, wic, W32, Q);
     if constexpr (W32 <= 4) {
       if (resident) {  // the same for the whole block
@@ -521,13 +542,13 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   constexpr int RS = rs_of_w32(W32);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int sb = slot_bytes(b.max_nodes, RS, 1, SUM, W32, Q);
+  const int sb = slot_bytes(b.max_nodes, RS, 1, kScratch<W32, SUM>, W32, Q);
   uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)wib * sb;
   uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
   volatile int *sflag = part + 24;
   SlotSum ss{};
-  if constexpr (SUM) {
+  if constexpr (kScratch<W32, SUM>) {
     ss = slot_sum(slot_base, b.max_nodes, RS, 1, 0, W32, Q);
     if constexpr (W32 <= 4) {
       // one dataset in this launch with its cells in registers: the block's

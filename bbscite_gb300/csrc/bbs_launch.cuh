@@ -25,8 +25,8 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   const int threads = 32 * a.wpc * cpb;
   if (threads > 128) return (int)cudaErrorInvalidConfiguration;
   const size_t smem =
-      (size_t)cpb * slot_bytes(a.ds.n_nodes, RS, a.wpc, SUM, W32, Q) +
-      table_bytes(a.ds.n_nodes, W32, Q, a.wpc, SUM);
+      (size_t)cpb * slot_bytes(a.ds.n_nodes, RS, a.wpc, kScratch<W32, SUM>, W32, Q) +
+      table_bytes(a.ds.n_nodes, W32, Q, a.wpc, kScratch<W32, SUM>);
   auto kern = mcmc_kernel<W32, Q, SUM, REC>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
@@ -47,8 +47,8 @@ int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   const int threads = 32 * wpb;
   const size_t smem =
-      (size_t)wpb * slot_bytes(b.max_nodes, RS, 1, SUM, W32, Q) +
-      (b.table_ds >= 0 ? table_bytes(b.max_nodes, W32, Q, 1, SUM) : 0);
+      (size_t)wpb * slot_bytes(b.max_nodes, RS, 1, kScratch<W32, SUM>, W32, Q) +
+      (b.table_ds >= 0 ? table_bytes(b.max_nodes, W32, Q, 1, kScratch<W32, SUM>) : 0);
   auto kern = batch_kernel<W32, Q, SUM>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
