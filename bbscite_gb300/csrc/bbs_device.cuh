@@ -810,10 +810,11 @@ __device__ __forceinline__ void propose_parents(const uint8_t *cur,
   __syncwarp();
 }
 
-// Checked builds: every non-root node's row is its parent's row plus the
-// node itself.
+// Whether `par` is the parent vector of the rows: every non-root node's row
+// is its parent's row plus the node itself.  Once per evaluation, so out of
+// line.
 template <int W32>
-__device__ __forceinline__ bool parents_match_rows(const uint32_t *rows, int n,
+__device__ __noinline__ bool parents_match_rows(const uint32_t *rows, int n,
                                                    const uint8_t *par,
                                                    int lane) {
   constexpr int RS = rs_of_w32(W32);
