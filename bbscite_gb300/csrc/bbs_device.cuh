@@ -212,6 +212,8 @@ struct Realized {
   bbs_move_params p;
   int ndv, ndw;   // descendant counts of v and w (v, w included)
   bool related;   // w is an ancestor of v
+  bool fallback;  // a k-th (non)descendant index reached its count: the
+                  // reference's rule then takes node 0
 };
 
 // Descendant sets of v and w as warp-uniform bit sets (one ballot per node
@@ -309,6 +311,7 @@ __device__ __forceinline__ Realized realize_move(const uint32_t *rows, int n,
   R.ndv = ndv;
   R.ndw = ndw;
   R.related = has_bit<W32>(Dw, v);
+  R.fallback = i_desc >= (uint32_t)ndv || i_nondesc >= (uint32_t)nnd;
   return R;
 }
 

@@ -246,6 +246,7 @@ __device__ __forceinline__ void run_chain(
     float corr = 1.0f;
     float fa = 0.0f, fb = 0.0f, ta = 0.0f, tb = 0.0f;
     ErrorGeom geo{};  // of the current state, on learned error moves
+    bool fallback_move = false;  // the realised move took node 0 by fallback
     uint32_t Dv[W32], Dw[W32];
     if (!err_move) {
       const Realized R = realize_move<W32>(cur, n, beta, raw, lane, Dv, Dw);
@@ -257,6 +258,7 @@ __device__ __forceinline__ void run_chain(
       }
       build_proposal<W32>(cur, prop, n, R.p, Dv, Dw, R.related, wpc, wic,
                           lane);
+      fallback_move = R.fallback;
       if (cur_par_ok && wic == 0)
         propose_parents(cpar, ppar, n, R.p, R.related, lane);
       scored = prop;
@@ -291,13 +293,30 @@ __device__ __forceinline__ void run_chain(
       beta_terms_f(ds, pbeta, PL.l01, PL.l11, pprior);
     }
     if (multi) __syncthreads(); else __syncwarp();
-    // the evaluated tree's parent vector, used only where it checks out
-    // against the rows (so the counts never depend on how it was found)
+    // The evaluated tree's parent vector.  It is checked against the rows
+    // where it can be wrong -- a proposal whose move took node 0 by
+    // fallback, and any tree of a multi-warp chain -- and used only where it
+    // checks out; checked builds check every one and record a mismatch
+    // outside those cases as a failed device check.
     bool par_ok = false;
     if constexpr (W32 <= 4) {
-      if (cpar != nullptr && cur_par_ok)
-        par_ok = parents_match_rows<W32>(scored, n, scored == cur ? cpar : ppar,
-                                         lane);
+      if (cpar != nullptr && cur_par_ok) {
+        const bool suspect = multi || (scored != cur && fallback_move);
+        bool check = suspect;
+#ifdef BBS_CHECKED
+        check = true;
+#endif
+        par_ok = true;
+        if (check) {
+          par_ok = parents_match_rows<W32>(scored, n,
+                                           scored == cur ? cpar : ppar, lane);
+#ifdef BBS_CHECKED
+          if (!suspect)
+            device_check(par_ok, status, kCheckParent,
+                         (uint32_t)raw.move_type, 4u);
+#endif
+        }
+      }
     }
     sx.par = par_ok ? (scored == cur ? cpar : ppar) : nullptr;
     const bool prop_par_ok = par_ok && scored != cur;
