@@ -307,3 +307,55 @@ def test_quality_fixture_scores(orc):
         r, _, _, _ = orc.logscore_tree(w["alpha"], w["beta"], w["beta_sd"],
                                        dm, mut, known, w["beta"])
         assert np.float32(r) == np.float32(row["best_score"])
+
+
+def _index_reached_count(am, mp, raw) -> bool:
+    """Whether a realised move's k-th (non)descendant index reached its
+    count: floor(u * count) in float (src/MutationTree.hpp:341-344), the
+    case in which the reference's selection returns node 0."""
+    n = am.shape[0]
+    v = int(mp["v"])
+    nd = sum(bin(int(am[v, k])).count("1") for k in range(am.shape[1]))
+    nn = n - nd
+    i_d = int(np.floor(np.float32(raw["raw_descendant_of_v"]) * np.float32(nd)))
+    i_n = int(np.floor(np.float32(raw["raw_nondescendant_of_v"]) *
+                       np.float32(nn)))
+    return i_d >= nd or i_n >= nn
+
+
+def test_parent_vector_moves_except_node0_fallbacks(orc):
+    """The GPU's inherited counts follow each move on the parent vector, as
+    the reference's test restates the moves (test/MutationTree.cpp:697-735).
+    That form agrees with the reference's row update for every move except
+    one whose k-th (non)descendant index reached its count: the reference
+    then takes node 0, which need not be a (non)descendant of v.  The
+    kernels flag exactly those moves and check their parent vectors against
+    the rows.  Raw uniforms of 1.0 (edge values the golden move streams
+    hold too) make the case certain."""
+    rng = np.random.default_rng(97)
+    top = np.float32(1.0)
+    flagged = mismatched = 0
+    for trial in range(12):
+        G = int(rng.integers(4, 70))
+        pv = D.random_parent_vector(rng, G)
+        am, dm = orc.parent_to_matrix(pv)
+        mp_probs = orc.move_probs(0.0, 0.4, 0.2, 0.4)
+        raws = orc.sample_moves(mp_probs, G + 1, 500 + trial, 0, 300)
+        edge = rng.random(len(raws)) < 0.3
+        raws["raw_descendant_of_v"][edge] = top
+        raws["raw_nondescendant_of_v"][edge] = top
+        for raw in raws:
+            mp = orc.realize(am, dm, 0.3, raw)
+            if int(mp["move_type"]) == 0:
+                continue
+            nam, ndm, _ = orc.apply_move(am, dm, 0.3, mp)
+            exp = _parent_vector_move(orc.parent_vector(dm), mp, am)
+            agree = list(exp) == list(orc.parent_vector(ndm)) and (
+                ndm == orc.parent_to_matrix(exp)[1]).all()
+            if _index_reached_count(am, mp, raw):
+                flagged += 1
+                mismatched += not agree
+            else:
+                assert agree, (trial, mp)
+                am, dm = nam, ndm  # advance along proper moves: trees only
+    assert flagged > 0 and mismatched > 0
