@@ -295,9 +295,9 @@ __device__ __forceinline__ void run_chain(
     if (multi) __syncthreads(); else __syncwarp();
     // The evaluated tree's parent vector.  It is checked against the rows
     // where it can be wrong -- a proposal whose move took node 0 by
-    // fallback, and any tree of a multi-warp chain -- and used only where it
-    // checks out; checked builds check every one and record a mismatch
-    // outside those cases as a failed device check.
+    // fallback -- and, conservatively, on every tree of a multi-warp chain,
+    // and used only where it checks out; checked builds check every one and
+    // record a mismatch outside those cases as a failed device check.
     bool par_ok = false;
     if constexpr (W32 <= 4) {
       if (cpar != nullptr && cur_par_ok) {

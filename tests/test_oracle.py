@@ -359,3 +359,42 @@ def test_parent_vector_moves_except_node0_fallbacks(orc):
                 assert agree, (trial, mp)
                 am, dm = nam, ndm  # advance along proper moves: trees only
     assert flagged > 0 and mismatched > 0
+
+
+def test_golden_chains_parent_vector_mismatches_are_node0_fallbacks(orc,
+                                                                    golden):
+    """Along the reference's own recorded chains (its move streams and its
+    accept decisions), the parent-vector form of a move disagrees with the
+    row update only at moves whose k-th (non)descendant index reached its
+    count -- the moves the kernels flag and check.  The first such
+    disagreements of the four chains are steps 73, 153, none and 585.  A
+    chain's cells held in registers (the launches whose warps hold all its
+    cells) are the only ones scored from parent vectors, which is why a
+    wrong vector shows at those steps only where the launch keeps the cells
+    resident."""
+    first = []
+    for ci in range(len(golden["chain_cases"])):
+        raws = golden[f"chain{ci}_raw"]
+        acc = golden[f"chain{ci}_accepted"]
+        am, dm = orc.parent_to_matrix(golden[f"chain{ci}_start"])
+        beta = 0.2
+        bad = []
+        for i, raw in enumerate(raws):
+            mp = orc.realize(am, dm, beta, raw)
+            if int(mp["move_type"]) == 0:
+                if acc[i]:
+                    beta = float(mp["new_beta"])
+                continue
+            nam, ndm, _ = orc.apply_move(am, dm, beta, mp)
+            pv = orc.parent_vector(dm)
+            is_tree = (orc.parent_to_matrix(pv)[1] == dm).all()
+            exp = _parent_vector_move(pv, mp, am)
+            agree = list(exp) == list(orc.parent_vector(ndm)) and (
+                ndm == orc.parent_to_matrix(exp)[1]).all()
+            if is_tree and not agree:
+                assert _index_reached_count(am, mp, raw), (ci, i)
+                bad.append(i)
+            if acc[i]:
+                am, dm = nam, ndm
+        first.append(bad[0] if bad else None)
+    assert first == [73, 153, None, 585]
