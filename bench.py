@@ -278,7 +278,12 @@ def run_reference(args) -> None:
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64-popcount+f32", "data": "synthetic",
         "config": {"workload": f"{w['n_genes']} genes x {w['n_cells']} "
-                   "cells, plain MCMC, fixed error rates",
+                   f"cells, {args.chains} chains; data alpha=1e-3 beta=0.2 "
+                   "(10% unknown, 2% homozygous); the reference's plain "
+                   "MCMC at fixed error rates (it has no batched or adjoint "
+                   "form)",
+                   "n_genes": w["n_genes"], "n_cells": w["n_cells"],
+                   "chains": args.chains,
                    "parallelism": "host threads over chains"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"],
                          "kind": info["kind"], "sample": info["sample"]},
