@@ -287,6 +287,29 @@ def test_sumscore_gradient_fd(orc):
         np.testing.assert_allclose(post.sum(axis=1), 1.0, rtol=1e-12)
 
 
+def test_golden_vectors_regenerate_bit_for_bit(orc, tmp_path):
+    """tests/golden/ref_vectors.npz is exactly what its generator makes from
+    the reference's own classes (oracle/_ref), array for array.  Needs the
+    reference build, which exists only where the reference sources do."""
+    import importlib.util
+    import os
+    if orc.ref_lib() is None:
+        pytest.skip("oracle/_ref is not built here")
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location(
+        "make_golden", os.path.join(here, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    mg.OUT = str(tmp_path / "ref_vectors.npz")
+    mg.main()
+    old = np.load(os.path.join(here, "ref_vectors.npz"))
+    new = np.load(mg.OUT)
+    assert sorted(old.files) == sorted(new.files)
+    for k in old.files:
+        assert old[k].dtype == new[k].dtype and old[k].shape == new[k].shape, k
+        assert old[k].tobytes() == new[k].tobytes(), k
+
+
 def test_quality_fixture_scores(orc):
     """The committed reference results of the quality comparison are the
     reference's cell-order scores of their best trees."""
