@@ -75,12 +75,13 @@ __host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
 }
 
 // The sum-score pieces of a slot: parent vectors and warp wic's scratch.
+// (Host-callable too: the layout test walks it over every shape.)
 struct SlotSum {
   uint8_t *par0, *par1;
   SumCtx sx;
 };
 
-__device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n, int rs,
+__host__ __device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n, int rs,
                                             int wpc, int wic, int w32, int q) {
   SlotSum o{};
   uint8_t *p = slot + 4 * (2 * n * rs + 24 * wpc + 4);

@@ -1,0 +1,137 @@
+// Shared-memory layout of the chain kernels, walked on the host over every
+// shape the launchers accept: node counts 2..256, 1..4 cells per lane,
+// 1..4 warps per chain (one-warp chains 1..4 per block), both scores.  For
+// each chain slot the pieces the kernels address -- the two row buffers,
+// both parities of the per-warp partial sums, the flag word, the parent
+// vectors, and each warp's node order, depth histogram and count table --
+// must lie inside the slot, be disjoint and be aligned for their element
+// type; the block's increment table must lie after the slots and inside the
+// launch's dynamic shared memory.  Prints "layout ok <cases>" or the first
+// violation (exit status 1).
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include "bbs_kernels.cuh"
+
+namespace {
+
+struct Piece {
+  const char *name;
+  size_t lo, hi;  // byte offsets [lo, hi) from the block's base
+  size_t align;
+};
+
+long g_cases = 0;
+
+bool fail(const char *what, int n, int q, int wpc, int cpb, bool sum,
+          const char *a, const char *b = "") {
+  std::printf("FAIL %s: n=%d q=%d wpc=%d cpb=%d sum=%d %s %s\n", what, n, q,
+              wpc, cpb, (int)sum, a, b);
+  return false;
+}
+
+// One launch: cpb slots of wpc warps, the table after them.  `table` says
+// whether the launch builds an increment table (plain kernel: always with
+// the scratch; batched kernel: when a launch group holds one dataset).
+bool check(int n, int q, int wpc, int cpb, bool sum, bool table) {
+  const int w32 = bbs::w32_of_nodes(n);
+  const int rs = bbs::rs_of_w32(w32);
+  const bool scratch = sum || w32 <= 4;  // kScratch<W32, SUM>
+  const int sb = bbs::slot_bytes(n, rs, wpc, scratch, w32, q);
+  const size_t tb =
+      table ? (size_t)bbs::table_bytes(n, w32, q, wpc, scratch) : 0;
+  const size_t total = (size_t)cpb * sb + tb;
+  std::vector<uint8_t> smem(total + 16);
+  uint8_t *base = smem.data();
+  std::vector<Piece> all;
+  if (sb % 16 != 0) return fail("slot size not a multiple of 16", n, q, wpc, cpb, sum, "");
+  for (int s = 0; s < cpb; s++) {
+    const size_t o = (size_t)s * sb;
+    const size_t first = all.size();  // this slot's pieces start here
+    const size_t rows = (size_t)4 * 2 * n * rs;
+    const size_t part = o + rows;
+    all.push_back({"rows", o, o + rows, 16});
+    // partial sums: max score 12 words per warp and parity, read as ints
+    // at [12 w] and [12 w + 1]; sum score 6 long longs per warp and parity
+    const size_t pmax = (size_t)4 * (12 * wpc + 12 * (wpc - 1) + 2);
+    const size_t psum = (size_t)8 * (6 * wpc + 6 * (wpc - 1) + 6);
+    all.push_back({"partials", part, part + (sum ? psum : pmax), sum ? 8u : 4u});
+    const size_t flag = part + (size_t)4 * 24 * wpc;
+    if ((sum ? part + psum : part + pmax) > flag)
+      return fail("partials overrun the flag", n, q, wpc, cpb, sum, "");
+    all.push_back({"flag", flag, flag + 4, 4});
+    if (scratch) {
+      for (int wic = 0; wic < wpc; wic++) {
+        const bbs::SlotSum ss =
+            bbs::slot_sum(base + o, n, rs, wpc, wic, w32, q);
+        auto off = [&](const void *p) {
+          return (size_t)(static_cast<const uint8_t *>(p) - base);
+        };
+        if (wic == 0) {
+          all.push_back({"par0", off(ss.par0), off(ss.par0) + n, 1});
+          all.push_back({"par1", off(ss.par1), off(ss.par1) + n, 1});
+        }
+        all.push_back({"ord", off(ss.sx.ord), off(ss.sx.ord) + 2 * n, 2});
+        // the histogram doubles as the depth scratch of the parent
+        // derivation: n ints at least
+        const size_t hist = (size_t)4 * 32 * ((n + 31) / 32);
+        if (hist < (size_t)4 * n)
+          return fail("histogram smaller than n ints", n, q, wpc, cpb, sum, "");
+        all.push_back({"hist", off(ss.sx.hist), off(ss.sx.hist) + hist, 4});
+        if (w32 <= 4) {
+          if (ss.sx.cnt == nullptr)
+            return fail("no count table", n, q, wpc, cpb, sum, "");
+          all.push_back({"cnt", off(ss.sx.cnt),
+                         off(ss.sx.cnt) + (size_t)2 * n * q * 32, 2});
+        } else if (ss.sx.cnt != nullptr) {
+          return fail("count table for wide rows", n, q, wpc, cpb, sum, "");
+        }
+      }
+    }
+    for (size_t i = first; i < all.size(); i++)
+      if (all[i].lo < o || all[i].hi > o + sb)
+        return fail("piece outside its slot", n, q, wpc, cpb, sum, all[i].name);
+  }
+  if (table && scratch && w32 <= 4) {
+    const size_t lo = (size_t)cpb * sb;
+    const size_t need = (size_t)2 * n * 32 * q * wpc;
+    if (tb < need)
+      return fail("increment table too small", n, q, wpc, cpb, sum, "");
+    all.push_back({"table", lo, lo + need, 16});
+  }
+  for (size_t i = 0; i < all.size(); i++) {
+    if (all[i].hi > total)
+      return fail("piece past the launch's shared memory", n, q, wpc, cpb,
+                  sum, all[i].name);
+    if (all[i].lo % all[i].align != 0)
+      return fail("misaligned piece", n, q, wpc, cpb, sum, all[i].name);
+    for (size_t j = i + 1; j < all.size(); j++)
+      if (all[i].lo < all[j].hi && all[j].lo < all[i].hi)
+        return fail("overlapping pieces", n, q, wpc, cpb, sum, all[i].name,
+                    all[j].name);
+  }
+  g_cases++;
+  return true;
+}
+
+}  // namespace
+
+int main() {
+  for (int n = 2; n <= 256; n++)
+    for (int q = 1; q <= bbs::kMaxQ; q++)
+      for (int sum = 0; sum < 2; sum++) {
+        // plain kernel: one-warp chains 1..4 per block, or one chain of
+        // 2..4 warps; its table whenever the slots carry the scratch
+        for (int cpb = 1; cpb <= 4; cpb++)
+          if (!check(n, q, 1, cpb, sum != 0, true)) return 1;
+        for (int wpc = 2; wpc <= 4; wpc++)
+          if (!check(n, q, wpc, 1, sum != 0, true)) return 1;
+        // batched kernel: one-warp slots, with or without the table
+        for (int wpb = 1; wpb <= 4; wpb++)
+          for (int table = 0; table < 2; table++)
+            if (!check(n, q, 1, wpb, sum != 0, table != 0)) return 1;
+      }
+  std::printf("layout ok %ld\n", g_cases);
+  return 0;
+}

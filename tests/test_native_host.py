@@ -134,3 +134,23 @@ def test_create_validates_arguments(native):
     with pytest.raises(native.BbsError) as e:
         native.Context(mut, mut, 4, 10, p)
     assert "sum of the move type probabilities is zero" in str(e.value)
+
+
+def test_shared_memory_layout_of_every_launch_shape(tmp_path):
+    """tests/cpp/layout_probe.cu walks the chain kernels' shared-memory
+    layout (the slot and table sizes and the per-warp pieces the kernels
+    address) over every node count, cells per lane, warps per chain and
+    chains per block that the launchers accept: every piece lies inside its
+    slot, the pieces are disjoint and aligned, and the increment table fits
+    after the slots."""
+    import subprocess
+    from bbscite_gb300 import build as B
+    exe = str(tmp_path / "layout_probe")
+    subprocess.run([B.nvcc(), *B.ARCH, "-std=c++17", "-I" + B.INCLUDE,
+                    "-I" + B.CSRC,
+                    os.path.join(ROOT, "tests", "cpp", "layout_probe.cu"),
+                    "-o", exe], check=True, capture_output=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout
+    assert r.stdout.startswith("layout ok "), r.stdout
+    assert int(r.stdout.split()[2]) == 255 * 4 * 2 * 15
