@@ -5,6 +5,8 @@
 * golden vectors produced by the reference's own headers
   (tests/golden/ref_vectors.npz, tests/golden/make_golden.py);
 * the fuzz property of test/MutationTree.cpp:663-744 with fixed seeds;
+* the end-to-end test of test/Application.cpp:38-143 on the restated
+  step loop;
 * the FP64 sum-score gradient against central finite differences.
 """
 import math
@@ -421,3 +423,24 @@ def test_golden_chains_parent_vector_mismatches_are_node0_fallbacks(orc,
                 am, dm = nam, ndm
         first.append(bad[0] if bad else None)
     assert first == [73, 153, None, 585]
+
+
+def test_application_kat_on_the_oracle(orc, kat):
+    """The reference's end-to-end test (test/Application.cpp:38-143) on the
+    oracle's restated step loop, in the reference's cell-order score: over
+    the test's chain count and chain length, the best tree found scores
+    like the true tree."""
+    k = kat["application"]
+    mut = np.array([[int(s, 2)] for s in k["is_mutated"]], dtype=np.uint64)
+    known = np.array([[int(s, 2)] for s in k["is_known"]], dtype=np.uint64)
+    rng = np.random.default_rng(38)
+    parents = np.stack([D.random_parent_vector(rng, k["n_genes"])
+                        for _ in range(k["n_chains"])])
+    mp = orc.move_probs(beta_sd=k["beta_sd"])
+    best, _ = orc.run_chains_mt(k["alpha"], k["beta"], k["beta_sd"], 1.0, mp,
+                                143, parents, mut, known, k["chain_length"],
+                                k["n_chains"], score_mode=0)
+    _, dm = orc.parent_to_matrix(np.array(k["true_parent_vector"]))
+    r, _, _, _ = orc.logscore_tree(k["alpha"], k["beta"], k["beta_sd"], dm,
+                                   mut, known, k["beta"])
+    assert best == pytest.approx(float(r), rel=1e-5)
