@@ -154,3 +154,43 @@ def test_shared_memory_layout_of_every_launch_shape(tmp_path):
     assert r.returncode == 0, r.stdout
     assert r.stdout.startswith("layout ok "), r.stdout
     assert int(r.stdout.split()[2]) == 255 * 4 * 2 * 15
+
+
+def _ctype_of(decl: str):
+    """The ctypes type a C parameter or return declaration passes as."""
+    d = " ".join(decl.replace("const ", "").split())
+    if "*" in d:
+        return C.c_char_p if d.startswith("char") else C.c_void_p
+    base = d.split()[0] if d else "void"
+    return {"void": None, "int": C.c_int, "int32_t": C.c_int32,
+            "uint32_t": C.c_uint32, "uint64_t": C.c_uint64,
+            "float": C.c_float, "size_t": C.c_size_t}[base]
+
+
+def test_binding_signatures_match_the_header(native):
+    """Every entry point the Python binding declares passes the argument
+    count and scalar widths that include/bbscite_gb300.h declares (a drift
+    between the two would pass wrong values silently through ctypes)."""
+    with open(os.path.join(ROOT, "include", "bbscite_gb300.h")) as f:
+        text = re.sub(r"/\*.*?\*/|//[^\n]*", "", f.read(), flags=re.S)
+    decls = {}
+    for ret, name, params in re.findall(
+            r"BBS_API\s+([^;()]*?)\b(bbs_\w+)\s*\(([^)]*)\)\s*;", text):
+        ps = [p.strip() for p in params.split(",")]
+        if ps == ["void"]:
+            ps = []
+        # the parameter's type is the declaration less its name
+        types = [re.sub(r"\b\w+\s*$", "", p) if not p.endswith("*") else p
+                 for p in ps]
+        decls[name] = (_ctype_of(ret.strip()), [_ctype_of(t) for t in types])
+    L = native.lib()
+    bound = [n for n in decls if getattr(L, n).argtypes is not None]
+    assert len(bound) >= 40
+    for name in bound:
+        fn = getattr(L, name)
+        want_ret, want_args = decls[name]
+        # any pointer passes as a pointer; only returned strings decode
+        ptr = (C.c_void_p, C.c_char_p)
+        got = ["ptr" if t in ptr else t for t in fn.argtypes]
+        assert got == ["ptr" if t in ptr else t for t in want_args], name
+        assert fn.restype == want_ret, name
