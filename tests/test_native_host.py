@@ -194,3 +194,31 @@ def test_binding_signatures_match_the_header(native):
         got = ["ptr" if t in ptr else t for t in fn.argtypes]
         assert got == ["ptr" if t in ptr else t for t in want_args], name
         assert fn.restype == want_ret, name
+
+
+def test_product_code_never_reaches_the_oracle():
+    """The package is the product: no module of bbscite_gb300/ imports the
+    oracle (test infrastructure), and no native source includes or loads
+    anything from oracle/.  Only tests, the smoke check and the bench's CPU
+    baseline use it, as the checker."""
+    import ast
+    pkg = os.path.join(ROOT, "bbscite_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for fn in files:
+            path = os.path.join(dirpath, fn)
+            if fn.endswith(".py"):
+                with open(path) as f:
+                    tree = ast.parse(f.read(), path)
+                for node in ast.walk(tree):
+                    names = []
+                    if isinstance(node, ast.Import):
+                        names = [a.name for a in node.names]
+                    elif isinstance(node, ast.ImportFrom):
+                        names = [node.module or ""]
+                    assert not any(n.split(".")[0] == "oracle"
+                                   for n in names), path
+            elif fn.endswith((".cu", ".cuh", ".h", ".cpp", ".hpp")):
+                with open(path) as f:
+                    text = f.read()
+                assert not re.search(r'#include\s+[<"][^">]*oracle', text), path
+                assert "libbbs_oracle" not in text and "liboracle" not in text, path
