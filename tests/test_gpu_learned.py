@@ -299,3 +299,120 @@ def test_extreme_sizes_and_rates_replay_in_fp64(native, orc, G, Cn, alpha,
     amb = sum(replay(orc, native, m, p, starts[ch], tr[ch], final["dm"][ch])
               for ch in range(chains))
     assert amb <= 2
+
+
+# ---------------------------------------------------------------------
+# The headline path: the sum score with counts inherited from the parent
+# (rows of up to four words, cells held in registers, one warp per chain),
+# replayed step by step in FP64, and the batched launch of one dataset
+# shown to compute the same chains bit for bit.
+# ---------------------------------------------------------------------
+
+def _headline_params(native, move="langevin", p_err=0.1, seed=0xB5C17E):
+    """The bench's batched+adjoint chains: sum score, learned error rates
+    from the wrong start alpha=1e-2, beta=0.3."""
+    return native.default_params(
+        alpha_mean=1e-2, beta_mean=0.3, seed=seed, prob_beta_change=p_err,
+        score_mode=native.SCORE_SUM,
+        error_move=getattr(native, "ERROR_" + move.upper()))
+
+
+@pytest.mark.parametrize("G,Cn,q", [(40, 50, 2), (95, 96, 3), (127, 64, 2)])
+@pytest.mark.parametrize("move,p_err", [("langevin", 0.1),
+                                        ("random_walk", 0.25)])
+def test_inherited_count_chains_replay_in_fp64(native, orc, G, Cn, q, move,
+                                               p_err):
+    """Sum-score chains whose node loop inherits counts from the parent:
+    41, 96 and 128 nodes (rows of 2, 3 and 4 32-bit words), every cell in
+    registers (q cells per lane, one warp per chain, four chains per
+    block -- at 95 x 96 the launch shape of the batched headline).  Each
+    step is replayed in FP64: realised move, proposed rows, the sum score
+    and the max score carried with it, the learned-rate proposal and the
+    decision."""
+    m, _, _ = D.generate_dataset(1000 + G, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    p = _headline_params(native, move, p_err, seed=0xB5C17E + G)
+    chains, steps = 4, 250
+    rng = np.random.default_rng(G + Cn)
+    starts = np.stack([D.random_parent_vector(rng, G) for _ in range(chains)])
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(chains, starts)
+        c.set_launch(q, 1, 4)
+        assert c.launch() == (q, 1, 4)
+        tr = c.run(steps, trace=True)
+        final = c.chains()
+    assert int((tr["move"]["move_type"] == 0).sum()) > 0
+    assert int(tr["accepted"].sum()) > 0
+    for ch in range(chains):
+        assert replay(orc, native, m, p, starts[ch], tr[ch],
+                      final["dm"][ch]) <= 2
+
+
+def test_headline_batch_equals_replayed_chains(native, orc):
+    """The batched launch of the bench's headline shape -- one 95 x 96
+    dataset, 3 cells per lane, 4-warp blocks, the dataset's increment table
+    built in the block -- leaves every chain (rows, best proposal and
+    state) bit-identical to the same chains run alone with a trace, and
+    those traced chains replay step by step in FP64."""
+    G, Cn = 95, 96
+    m, _, _ = D.generate_dataset(2026, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    p = _headline_params(native)
+    chains, steps = 8, 300
+    with native.Batch([(mut, known, Cn, G)], p) as b:
+        b.init_chains(chains)
+        b.set_launch(3, 4, 0)
+        assert b.launch()[:2] == (3, 4)
+        b.run(steps)
+        img_b = b.save_chains()
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(chains)
+        c.set_launch(3, 1, 4)
+        starts = np.stack([native.matrix_to_parent(d)
+                           for d in c.chains()["dm"]])
+        tr = c.run(steps, trace=True)
+        final = c.chains()
+        img_c = c.save_chains()
+    # both images end with the rows, the best proposals and the states of
+    # the chains in the same layout
+    n, W = G + 1, native.words(G + 1)
+    tail = 2 * chains * n * W * 8 + 128 * chains
+    assert img_b[-tail:] == img_c[-tail:]
+    for ch in range(chains):
+        assert replay(orc, native, m, p, starts[ch], tr[ch],
+                      final["dm"][ch]) <= 2
+
+
+@pytest.mark.parametrize("G,Cn", [(95, 96), (40, 200), (127, 64)])
+def test_sum_launch_shapes_give_identical_chains(native, G, Cn):
+    """Sum-score chains with learned rates are bit-identical under every
+    launch shape: inherited counts (cells in registers, one or several
+    warps per chain) and masked popcounts (streamed cells) add the same
+    terms in the same order."""
+    m, _, _ = D.generate_dataset(G + 5 * Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    shapes = [(3, 1, 4), (1, 1, 1), (2, 1, 2), (1, 2, 1), (1, 3, 1),
+              (2, 2, 1), (1, 4, 1), (4, 1, 1), (4, 2, 1)]
+    qmax = 2 if G + 1 > 128 else 4
+    outs = []
+    for q, wpc, cpb in shapes:
+        if q > qmax:
+            continue
+        p = _headline_params(native, seed=77)
+        with native.Context(mut, known, Cn, G, p) as c:
+            c.init_chains(9)
+            c.set_launch(q, wpc, cpb)
+            tr = c.run(150, trace=True)
+            outs.append((c.chains(), c.best(), tr))
+    ch0, b0, t0 = outs[0]
+    for ch, b, t in outs[1:]:
+        assert (ch["dm"] == ch0["dm"]).all()
+        np.testing.assert_array_equal(ch["score"], ch0["score"])
+        np.testing.assert_array_equal(ch["alpha"], ch0["alpha"])
+        np.testing.assert_array_equal(ch["beta"], ch0["beta"])
+        assert b["score"] == b0["score"] and (b["dm"] == b0["dm"]).all()
+        assert (t["accepted"] == t0["accepted"]).all()
+        np.testing.assert_array_equal(t["proposed_score"],
+                                      t0["proposed_score"])
+        np.testing.assert_array_equal(t["proposed_max_score"],
+                                      t0["proposed_max_score"])
