@@ -352,6 +352,7 @@ void prepare_dataset(const bbs_params *params, uint32_t n_cells,
   ds.lg_ab = logf(tgammaf(ds.bpa + ds.bpb));
   ds.lg_a = logf(tgammaf(ds.bpa));
   ds.lg_b = logf(tgammaf(ds.bpb));
+  ds.neg_zero = -0.0f;
   const float sum = params->prob_beta_change + params->prob_prune_n_reattach +
                     params->prob_swap_nodes + params->prob_swap_subtrees;
   const float pb = params->prob_beta_change / sum;
@@ -1930,6 +1931,8 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.max_nodes = grp.max_nodes;
     a.table_ds = grp.only_ds;
     const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;  // 1, 2 above 128 nodes
+    a.with_counts = grp.only_ds >= 0 &&
+                    inherits_counts(grp.w32, (int)b->n_cells[grp.only_ds], 32 * q);
     const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");
     BBS_CUDA(cudaEventRecord(b->side_ev[g], b->side[g]), "event");

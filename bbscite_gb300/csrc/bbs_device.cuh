@@ -402,6 +402,126 @@ __device__ __forceinline__ void build_proposal(const uint32_t *rows,
 }
 
 // ------------------------------------------------------------------------
+// Paired single precision (sm_100 and later): one instruction applies the
+// same IEEE round-to-nearest operation to both halves of a register pair,
+// with the results of two scalar instructions (no flush-to-zero), in half
+// the issue slots.  The node loops run two nodes of a cell side by side in
+// the two halves.  There is no paired multiply here: the compiler fuses a
+// paired multiply into a paired add that uses it, even with explicit
+// round-to-nearest modifiers (measured on GB300: the results equal the
+// fused form), so exact products are taken as fused multiply-adds of a
+// -0.0 addend that the compiler cannot see (pair_score_b2).
+// ------------------------------------------------------------------------
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\t"
+      "mov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 fadd2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+// max(a, b, c) in one instruction (sm_100 and later); exact, like fmaxf.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
+
+// ------------------------------------------------------------------------
+// Packed counts.  A lane's Q cells' counts of one node, d | m << 8 per cell
+// (d, m <= 255: a count of genes), two cells per 32-bit word: NW = (Q+1)/2
+// register words, word q/2 holding cell q in bits 16 (q & 1) upwards.
+// Adding two packed words adds every field at once (no field can carry
+// into the next).  A field becomes the exact biased float 2^23 + count
+// with one byte permute into the bit pattern 0x4B0000xx.  In shared memory
+// a table of entries [node][lane] keeps the Q/2 full words of an entry
+// together (one 32- or 64-bit access) and, for odd Q, the last cell's
+// field in a 16-bit table of its own: 2 Q bytes per entry.
+// ------------------------------------------------------------------------
+template <int Q>
+inline constexpr int kPackWords = (Q + 1) / 2;
+
+// A count table: full words at w, the odd cell's fields at h.
+template <typename W, typename H>
+struct PackTable {
+  W *w;
+  H *h;
+};
+using CountTable = PackTable<uint32_t, uint16_t>;
+using IncTable = PackTable<const uint32_t, const uint16_t>;
+
+// Table pointers for n nodes at `base` (2 Q n 32 bytes).
+template <typename T>
+__host__ __device__ inline T pack_table(void *base, int n, int q) {
+  T t;
+  t.w = reinterpret_cast<decltype(t.w)>(base);
+  t.h = reinterpret_cast<decltype(t.h)>(reinterpret_cast<uint8_t *>(base) +
+                                        (size_t)4 * (q / 2) * n * 32);
+  return t;
+}
+
+template <int Q, typename W, typename H>
+__device__ __forceinline__ void ld_pack(const PackTable<W, H> &t, int idx,
+                                        uint32_t (&k)[kPackWords<Q>]) {
+  constexpr int NP = Q / 2;
+  if constexpr (NP == 1) {
+    k[0] = t.w[idx];
+  } else if constexpr (NP == 2) {
+    const uint2 v = reinterpret_cast<const uint2 *>(t.w)[idx];
+    k[0] = v.x;
+    k[1] = v.y;
+  }
+  if constexpr ((Q & 1) != 0) k[NP] = t.h[idx];
+}
+
+template <int Q>
+__device__ __forceinline__ void st_pack(const CountTable &t, int idx,
+                                        const uint32_t (&k)[kPackWords<Q>]) {
+  constexpr int NP = Q / 2;
+  if constexpr (NP == 1) {
+    t.w[idx] = k[0];
+  } else if constexpr (NP == 2) {
+    reinterpret_cast<uint2 *>(t.w)[idx] = make_uint2(k[0], k[1]);
+  }
+  if constexpr ((Q & 1) != 0) t.h[idx] = (uint16_t)k[NP];
+}
+
+// Biased floats 2^23 + d and 2^23 + m of cell slot q (its word w = the
+// entry's word q / 2; q is a constant after unrolling).
+__device__ __forceinline__ float pack_d_biased(uint32_t w, int q) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7540u + 2u * (q & 1)));
+}
+__device__ __forceinline__ float pack_m_biased(uint32_t w, int q) {
+  return __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7541u + 2u * (q & 1)));
+}
+// The 16-bit field d | m << 8 of cell slot q.
+template <int NW>
+__device__ __forceinline__ uint32_t pack_field(const uint32_t (&k)[NW], int q) {
+  return (k[q >> 1] >> (16 * (q & 1))) & 0xFFFFu;
+}
+
+// ------------------------------------------------------------------------
 // Scoring (src/TreeScorer.hpp:131-210)
 // ------------------------------------------------------------------------
 // Population count of (X & A) over W32 words.  Groups of three words go
@@ -453,6 +573,33 @@ __device__ __forceinline__ float pair_score(int d, int m, float pdb,
   return pair_score_b(__int_as_float(0x4B000000 + d),
                       __int_as_float(0x4B000000 + m), pdb, pmb, l00, l01, l10,
                       l11);
+}
+
+// The log table duplicated into both halves of paired registers, with a
+// pair of -0.0 read from memory (DatasetDev::neg_zero).
+struct LogTable2 {
+  float2 l00, l01, l10, l11, nz;
+};
+
+// pair_score_b of two (cell, node) pairs side by side: the same four
+// products and three sums in the same order, rounded as the scalar form
+// rounds them.  Each product is a fused multiply-add of -0.0 (exactly the
+// rounded product); with the addend unknown at compile time the compiler
+// cannot fuse the product into the sum that follows, which it does with a
+// paired multiply and add whatever their rounding modifiers.
+__device__ __forceinline__ float2 pair_score_b2(float2 db, float2 mb,
+                                                float2 pdb, float2 pmb,
+                                                const LogTable2 &L) {
+  const float2 bias = dup2(8388608.0f);
+  const float2 f01 = fsub2(db, bias);
+  const float2 f11 = fsub2(mb, bias);
+  const float2 f00 = fsub2(pdb, db);
+  const float2 f10 = fsub2(pmb, mb);
+  float2 s = ffma2(f00, L.l00, L.nz);
+  s = fadd2(s, ffma2(f01, L.l01, L.nz));
+  s = fadd2(s, ffma2(f10, L.l10, L.nz));
+  s = fadd2(s, ffma2(f11, L.l11, L.nz));
+  return s;
 }
 
 // 64-bit hash of a tree's ancestor rows, the same in every lane: a mix of
@@ -529,7 +676,7 @@ template <int W32, int Q>
 __device__ __forceinline__ void best_nodes(const uint32_t *rows, int n,
                                            const Cells<W32, Q> &cb, float l00,
                                            float l01, float l10, float l11,
-                                           int (&bj)[Q]) {
+                                           float nz, int (&bj)[Q]) {
   constexpr int RS = rs_of_w32(W32);
   float best[Q];
   {
@@ -544,6 +691,7 @@ __device__ __forceinline__ void best_nodes(const uint32_t *rows, int n,
     }
   }
   int j = 1;
+  const LogTable2 L2{dup2(l00), dup2(l01), dup2(l10), dup2(l11), dup2(nz)};
 #pragma unroll 1
   for (; j + 1 < n; j += 2) {
     uint32_t a[W32], b[W32];
@@ -551,12 +699,15 @@ __device__ __forceinline__ void best_nodes(const uint32_t *rows, int n,
     ld_row<W32>(rows + (j + 1) * RS, b);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      const float s0 = pair_score(masked_popc<W32>(cb.D[q], a),
-                                  masked_popc<W32>(cb.M[q], a), cb.pdb[q],
-                                  cb.pmb[q], l00, l01, l10, l11);
-      const float s1 = pair_score(masked_popc<W32>(cb.D[q], b),
-                                  masked_popc<W32>(cb.M[q], b), cb.pdb[q],
-                                  cb.pmb[q], l00, l01, l10, l11);
+      const float2 db = make_float2(
+          __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)),
+          __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)));
+      const float2 mb = make_float2(
+          __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)),
+          __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)));
+      const float2 s2 = pair_score_b2(db, mb, dup2(cb.pdb[q]),
+                                      dup2(cb.pmb[q]), L2);
+      const float s0 = s2.x, s1 = s2.y;
       const bool up0 = s0 > best[q];
       best[q] = up0 ? s0 : best[q];
       bj[q] = up0 ? j : bj[q];
@@ -600,6 +751,11 @@ __device__ __forceinline__ void counts_at(const uint32_t *rows,
 struct LogTable {
   float l00, l10, l01, l11;
 };
+
+__device__ __forceinline__ LogTable2 log_table2(const LogTable &L, float nz) {
+  return LogTable2{dup2(L.l00), dup2(L.l01), dup2(L.l10), dup2(L.l11),
+                   dup2(nz)};
+}
 
 // Sum-over-attachments pass with its adjoint, for the lane's Q cells.
 // Per cell the scores s_j are summed as exp(s_j - r) against a reference r
@@ -664,9 +820,10 @@ __device__ __forceinline__ float ex2_approx(float t) {
 struct SumCtx {
   uint16_t *ord;        // [n]: node | parent << 8, in canonical order
   int *hist;            // [32 * ceil(n / 32)]: depth histogram, scratch
-  uint16_t *cnt;        // [n][Q][32]: packed counts d | m << 8, or null
-  const uint16_t *inc;  // [n][inc_stride]: per-gene increments, or null
-  int inc_stride;       // cell slots per increment row
+  CountTable cnt;       // [n][32]: every node's packed counts of the
+                        // lane's cells (cnt.w null: none)
+  IncTable inc;         // [n][32]: per-gene packed increments of the
+                        // warp's cells (inc.w null: none)
   const uint8_t *par;   // parent vector of the evaluated tree, or null
 };
 
@@ -840,87 +997,99 @@ __device__ __noinline__ bool parents_match_rows(const uint32_t *rows, int n,
   return __all_sync(BBS_FULL_MASK, ok);
 }
 
-// The increments of the block table for cell slot `slot` (cells
-// c0 + stride * q + lane index the table directly).
-__device__ __forceinline__ uint32_t gene_increment(const SumCtx &sx, int j,
-                                                   int slot) {
-  return sx.inc[j * sx.inc_stride + slot];
-}
-
-// The float work of two nodes for the lane's cells (both count sources
-// share it, so the sums are the same whichever found the counts).
-template <int Q>
-__device__ __forceinline__ void sum_pair(const float (&fd0)[Q],
-                                         const float (&fm0)[Q],
-                                         const float (&fd1)[Q],
-                                         const float (&fm1)[Q], float c1,
-                                         float c2, const float (&base)[Q],
-                                         float (&mx)[Q], float (&z)[Q],
-                                         float (&ed)[Q], float (&em)[Q]) {
-#pragma unroll
-  for (int q = 0; q < Q; q++) {
-    const float t0 = fmaf(fd0[q], c1, fmaf(fm0[q], c2, base[q]));
-    const float t1 = fmaf(fd1[q], c1, fmaf(fm1[q], c2, base[q]));
-    const float e0 = ex2_approx(t0), e1 = ex2_approx(t1);
-    mx[q] = fmaxf(mx[q], fmaxf(t0, t1));
-    z[q] += e0 + e1;
-    ed[q] = fmaf(e0, fd0[q], fmaf(e1, fd1[q], ed[q]));
-    em[q] = fmaf(e0, fm0[q], fmaf(e1, fm1[q], em[q]));
-  }
-}
-
-// Inherited counts of the nodes at order positions i and i + 1, stored in
-// the count table.  All four loads come first; when node i + 1 is node i's
-// child, its parent's counts are taken from the register instead of the
-// table (whose entry is not stored yet).
-template <int Q>
-__device__ __forceinline__ void inherit_pair(const SumCtx &sx, int i, int c0,
-                                             int stride, int lane,
-                                             uint32_t (&k0)[Q],
-                                             uint32_t (&k1)[Q], int &j0,
+// Inherited counts of the nodes at order positions i and i + 1, all Q
+// cells at once (packed), stored in the count table.  All four loads come
+// first; when node i + 1 is node i's child, its parent's counts are taken
+// from the register instead of the table (whose entry is not stored yet).
+template <int Q, int NW = kPackWords<Q>>
+__device__ __forceinline__ void inherit_pair(const SumCtx &sx, int i, int lane,
+                                             uint32_t (&k0)[NW],
+                                             uint32_t (&k1)[NW], int &j0,
                                              int &j1) {
   const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
   j0 = (int)(o0 & 0xFF);
   j1 = (int)(o1 & 0xFF);
   const int p0 = (int)(o0 >> 8), p1 = (int)(o1 >> 8);
-  uint32_t a0[Q], a1[Q], g0[Q], g1[Q];
+  uint32_t a0[NW], a1[NW], g0[NW], g1[NW];
+  ld_pack<Q>(sx.cnt, p0 * 32 + lane, a0);
+  ld_pack<Q>(sx.cnt, p1 * 32 + lane, a1);
+  ld_pack<Q>(sx.inc, j0 * 32 + lane, g0);
+  ld_pack<Q>(sx.inc, j1 * 32 + lane, g1);
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
-    a0[q] = sx.cnt[(p0 * Q + q) * 32 + lane];
-    a1[q] = sx.cnt[(p1 * Q + q) * 32 + lane];
-    g0[q] = gene_increment(sx, j0, c0 + stride * q + lane);
-    g1[q] = gene_increment(sx, j1, c0 + stride * q + lane);
+  for (int w = 0; w < NW; w++) {
+    k0[w] = a0[w] + g0[w];
+    k1[w] = (p1 == j0 ? k0[w] : a1[w]) + g1[w];
   }
+  st_pack<Q>(sx.cnt, j0 * 32 + lane, k0);
+  st_pack<Q>(sx.cnt, j1 * 32 + lane, k1);
+}
+
+// The same for the node at order position i alone.
+template <int Q, int NW = kPackWords<Q>>
+__device__ __forceinline__ void inherit_one(const SumCtx &sx, int i, int lane,
+                                            uint32_t (&k)[NW], int &j) {
+  const uint32_t o = sx.ord[i];
+  j = (int)(o & 0xFF);
+  const int p = (int)(o >> 8);
+  uint32_t a[NW], g[NW];
+  ld_pack<Q>(sx.cnt, p * 32 + lane, a);
+  ld_pack<Q>(sx.inc, j * 32 + lane, g);
+#pragma unroll
+  for (int w = 0; w < NW; w++) k[w] = a[w] + g[w];
+  st_pack<Q>(sx.cnt, j * 32 + lane, k);
+}
+
+// The sum score's float work of two nodes, side by side in the halves of
+// paired registers, for the lane's Q cells: t = base + d c1 + m c2, its
+// power of two, the running maximum of t, and the sums of 2^t, 2^t d and
+// 2^t m, each kept as two partial sums (the nodes in the .x halves and
+// those in the .y halves) that are added at the end.  Both count sources
+// call this, so the sums are the same whichever found the counts.
+template <int Q>
+__device__ __forceinline__ void sum_pair2(const float2 (&fd)[Q],
+                                          const float2 (&fm)[Q], float2 c1,
+                                          float2 c2, const float2 (&base)[Q],
+                                          float (&mx)[Q], float2 (&z)[Q],
+                                          float2 (&ed)[Q], float2 (&em)[Q]) {
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    k0[q] = a0[q] + g0[q];
-    k1[q] = (p1 == j0 ? k0[q] : a1[q]) + g1[q];
-    sx.cnt[(j0 * Q + q) * 32 + lane] = (uint16_t)k0[q];
-    sx.cnt[(j1 * Q + q) * 32 + lane] = (uint16_t)k1[q];
+    const float2 t = ffma2(fd[q], c1, ffma2(fm[q], c2, base[q]));
+    const float2 e = make_float2(ex2_approx(t.x), ex2_approx(t.y));
+    mx[q] = fmax3(mx[q], t.x, t.y);
+    z[q] = fadd2(z[q], e);
+    ed[q] = ffma2(e, fd[q], ed[q]);
+    em[q] = ffma2(e, fm[q], em[q]);
   }
 }
 
-template <int Q>
-__device__ __forceinline__ void counts_to_float(const uint32_t (&k)[Q],
-                                                float (&fd)[Q], float (&fm)[Q]) {
+// The exact float counts (d, m) of the lane's Q cells at two nodes from
+// their packed entries (node 0 in .x, node 1 in .y).
+template <int Q, int NW>
+__device__ __forceinline__ void pack_to_float2(const uint32_t (&k0)[NW],
+                                               const uint32_t (&k1)[NW],
+                                               float2 (&fd)[Q],
+                                               float2 (&fm)[Q]) {
+  const float2 bias = dup2(8388608.0f);
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    fd[q] = __int_as_float(0x4B000000 | (k[q] & 0xFFu)) - 8388608.0f;
-    fm[q] = __int_as_float(0x4B000000 | (k[q] >> 8)) - 8388608.0f;
+    fd[q] = fsub2(make_float2(pack_d_biased(k0[q >> 1], q),
+                              pack_d_biased(k1[q >> 1], q)), bias);
+    fm[q] = fsub2(make_float2(pack_m_biased(k0[q >> 1], q),
+                              pack_m_biased(k1[q >> 1], q)), bias);
   }
 }
 
-// sum_pair on two nodes' packed counts.
-template <int Q>
-__device__ __forceinline__ void sum_counts(const uint32_t (&k0)[Q],
-                                           const uint32_t (&k1)[Q], float c1,
-                                           float c2, const float (&base)[Q],
-                                           float (&mx)[Q], float (&z)[Q],
-                                           float (&ed)[Q], float (&em)[Q]) {
-  float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
-  counts_to_float<Q>(k0, fd0, fm0);
-  counts_to_float<Q>(k1, fd1, fm1);
-  sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+// sum_pair2 on two nodes' packed counts.
+template <int Q, int NW>
+__device__ __forceinline__ void sum_counts2(const uint32_t (&k0)[NW],
+                                            const uint32_t (&k1)[NW],
+                                            float2 c1, float2 c2,
+                                            const float2 (&base)[Q],
+                                            float (&mx)[Q], float2 (&z)[Q],
+                                            float2 (&ed)[Q], float2 (&em)[Q]) {
+  float2 fd[Q], fm[Q];
+  pack_to_float2<Q, NW>(k0, k1, fd, fm);
+  sum_pair2<Q>(fd, fm, c1, c2, base, mx, z, ed, em);
 }
 
 // Q floats, passed and returned by value.
@@ -945,22 +1114,23 @@ __device__ __noinline__ Resum<Q> resum_cells(const uint32_t *rows, int n,
                                              float c1, float c2,
                                              const QF<Q> base, unsigned bad) {
   constexpr int RS = rs_of_w32(W32);
+  constexpr int NW = kPackWords<Q>;
   Resum<Q> o;
 #pragma unroll
   for (int q = 0; q < Q; q++) o.z.v[q] = o.ed.v[q] = o.em.v[q] = 0.0f;
 #pragma unroll 1
   for (int i2 = 0; i2 < n; i2++) {
     const int j = (int)(sx.ord[i2] & 0xFF);
-    uint32_t a[W32];
+    uint32_t a[W32], k[NW];
     if constexpr (!INHERIT) ld_row<W32>(rows + j * RS, a);
+    if constexpr (INHERIT) ld_pack<Q>(sx.cnt, j * 32 + lane, k);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
       if (!((bad >> q) & 1u)) continue;
       float fd, fm;
       if constexpr (INHERIT) {
-        const uint32_t k = sx.cnt[(j * Q + q) * 32 + lane];
-        fd = __int_as_float(0x4B000000 | (k & 0xFFu)) - 8388608.0f;
-        fm = __int_as_float(0x4B000000 | (k >> 8)) - 8388608.0f;
+        fd = pack_d_biased(k[q >> 1], q) - 8388608.0f;
+        fm = pack_m_biased(k[q >> 1], q) - 8388608.0f;
       } else {
         fd = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
         fm = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
@@ -982,48 +1152,57 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           long long (&acc)[6],
                                           const SumCtx &sx) {
   constexpr int RS = rs_of_w32(W32);
+  constexpr int NW = kPackWords<Q>;
   const float c1 = (L.l01 - L.l00) * kLog2E;  // per counted observed-0 bit
   const float c2 = (L.l11 - L.l10) * kLog2E;  // per counted observed-1 bit
+  const float2 c1p = dup2(c1), c2p = dup2(c2);
   const float u0 = fmaxf(L.l00, L.l01), u1 = fmaxf(L.l10, L.l11);
-  float r[Q], base[Q], mx[Q], z[Q], ed[Q], em[Q];
+  float r[Q], base[Q], mx[Q];
+  float2 base2[Q], z2[Q], ed2[Q], em2[Q];
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
     r[q] = fmaf(pd, u0, pm * u1) - 72.0f;
     base[q] = (fmaf(pd, L.l00, pm * L.l10) - r[q]) * kLog2E;
+    base2[q] = dup2(base[q]);
   }
   // the root (ord[0]) has no counted bits: t = base
+  if constexpr (INHERIT) {
+    uint32_t zero[NW];
+#pragma unroll
+    for (int w = 0; w < NW; w++) zero[w] = 0u;
+    st_pack<Q>(sx.cnt, (int)(sx.ord[0] & 0xFF) * 32 + lane, zero);
+  }
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    if constexpr (INHERIT) sx.cnt[(((int)(sx.ord[0] & 0xFF)) * Q + q) * 32 + lane] = 0;
     mx[q] = base[q];
-    z[q] = ex2_approx(base[q]);
-    ed[q] = em[q] = 0.0f;
+    z2[q] = make_float2(ex2_approx(base[q]), 0.0f);
+    ed2[q] = em2[q] = make_float2(0.0f, 0.0f);
   }
-  // the other nodes two at a time: independent work for the scheduler
+  // the other nodes two at a time, in the two halves of paired registers
   int i = 1;
   if constexpr (INHERIT) {
     // counts one pair ahead of the float work, which hides the table's
     // load latency behind the previous pair's arithmetic; two pairs per
     // iteration, alternating between two register sets
     if (i + 1 < n) {
-      uint32_t kA[Q], kB[Q], kA1[Q], kB1[Q];
+      uint32_t kA0[NW], kA1[NW], kB0[NW], kB1[NW];
       int jA0, jA1, jB0, jB1;  // node numbers (the max score uses them)
-      inherit_pair<Q>(sx, i, c0, stride, lane, kA, kA1, jA0, jA1);
+      inherit_pair<Q>(sx, i, lane, kA0, kA1, jA0, jA1);
 #pragma unroll 1
       for (; i + 5 < n; i += 4) {
-        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
-        sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
-        inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1, jA0, jA1);
-        sum_counts<Q>(kB, kB1, c1, c2, base, mx, z, ed, em);
+        inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+        sum_counts2<Q, NW>(kA0, kA1, c1p, c2p, base2, mx, z2, ed2, em2);
+        inherit_pair<Q>(sx, i + 4, lane, kA0, kA1, jA0, jA1);
+        sum_counts2<Q, NW>(kB0, kB1, c1p, c2p, base2, mx, z2, ed2, em2);
       }
       if (i + 3 < n) {
-        inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
-        sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
-        sum_counts<Q>(kB, kB1, c1, c2, base, mx, z, ed, em);
+        inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+        sum_counts2<Q, NW>(kA0, kA1, c1p, c2p, base2, mx, z2, ed2, em2);
+        sum_counts2<Q, NW>(kB0, kB1, c1p, c2p, base2, mx, z2, ed2, em2);
         i += 4;
       } else {
-        sum_counts<Q>(kA, kA1, c1, c2, base, mx, z, ed, em);
+        sum_counts2<Q, NW>(kA0, kA1, c1p, c2p, base2, mx, z2, ed2, em2);
         i += 2;
       }
     }
@@ -1032,35 +1211,35 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     for (; i + 1 < n; i += 2) {
       const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
       const int j0 = (int)(o0 & 0xFF), j1 = (int)(o1 & 0xFF);
-      float fd0[Q], fm0[Q], fd1[Q], fm1[Q];
+      float2 fd[Q], fm[Q];
       uint32_t a[W32], b[W32];
       ld_row<W32>(rows + j0 * RS, a);
       ld_row<W32>(rows + j1 * RS, b);
 #pragma unroll
       for (int q = 0; q < Q; q++) {
-        fd0[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f;
-        fm0[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f;
-        fd1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f;
-        fm1[q] = __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f;
+        fd[q] = make_float2(
+            __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], a)) - 8388608.0f,
+            __int_as_float(0x4B000000 + masked_popc<W32>(cb.D[q], b)) - 8388608.0f);
+        fm[q] = make_float2(
+            __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], a)) - 8388608.0f,
+            __int_as_float(0x4B000000 + masked_popc<W32>(cb.M[q], b)) - 8388608.0f);
       }
-      sum_pair<Q>(fd0, fm0, fd1, fm1, c1, c2, base, mx, z, ed, em);
+      sum_pair2<Q>(fd, fm, c1p, c2p, base2, mx, z2, ed2, em2);
     }
   }
   if (i < n) {
-    const uint32_t o = sx.ord[i];
-    const int j = (int)(o & 0xFF);
     float fd[Q], fm[Q];
     if constexpr (INHERIT) {
-      const int p = (int)(o >> 8);
+      uint32_t k[NW];
+      int j;
+      inherit_one<Q>(sx, i, lane, k, j);
 #pragma unroll
       for (int q = 0; q < Q; q++) {
-        const uint32_t k = (uint32_t)sx.cnt[(p * Q + q) * 32 + lane] +
-                           gene_increment(sx, j, c0 + stride * q + lane);
-        sx.cnt[(j * Q + q) * 32 + lane] = (uint16_t)k;
-        fd[q] = __int_as_float(0x4B000000 | (k & 0xFFu)) - 8388608.0f;
-        fm[q] = __int_as_float(0x4B000000 | (k >> 8)) - 8388608.0f;
+        fd[q] = pack_d_biased(k[q >> 1], q) - 8388608.0f;
+        fm[q] = pack_m_biased(k[q >> 1], q) - 8388608.0f;
       }
     } else {
+      const int j = (int)(sx.ord[i] & 0xFF);
       uint32_t a[W32];
       ld_row<W32>(rows + j * RS, a);
 #pragma unroll
@@ -1074,14 +1253,18 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
       const float t = fmaf(fd[q], c1, fmaf(fm[q], c2, base[q]));
       const float e = ex2_approx(t);
       mx[q] = fmaxf(mx[q], t);
-      z[q] += e;
-      ed[q] = fmaf(e, fd[q], ed[q]);
-      em[q] = fmaf(e, fm[q], em[q]);
+      z2[q].x += e;
+      ed2[q].x = fmaf(e, fd[q], ed2[q].x);
+      em2[q].x = fmaf(e, fm[q], em2[q].x);
     }
   }
+  float z[Q], ed[Q], em[Q];
   bool bad[Q], any = false;
 #pragma unroll
   for (int q = 0; q < Q; q++) {
+    z[q] = z2[q].x + z2[q].y;
+    ed[q] = ed2[q].x + ed2[q].y;
+    em[q] = em2[q].x + em2[q].y;
     bad[q] = !(mx[q] >= -80.0f * kLog2E);
     any |= bad[q];
   }
@@ -1166,7 +1349,7 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
   if (resident) {
     bool inherit = false;
     if constexpr (W32 <= 4)
-      inherit = sx.cnt != nullptr && sx.inc != nullptr && sx.par != nullptr;
+      inherit = sx.cnt.w != nullptr && sx.inc.w != nullptr && sx.par != nullptr;
     if (inherit) {
       if constexpr (W32 <= 4)
         sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
@@ -1208,86 +1391,101 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
 // lower index wins, which is what std::max over the nodes in index order
 // keeps (src/TreeScorer.hpp:187-193) -- so the chosen nodes, and the class
 // counts at them, are those of best_nodes.
-template <int Q>
-__device__ __forceinline__ void max_update(const uint32_t (&k)[Q], int j,
-                                           const float (&pdb)[Q],
-                                           const float (&pmb)[Q],
-                                           const LogTable &L,
-                                           float (&best)[Q], int (&bj)[Q]) {
+__device__ __forceinline__ void max_select(float s, int j, float &best,
+                                           int &bj) {
+  const bool up = s > best || (s == best && j < bj);
+  best = up ? s : best;
+  bj = up ? j : bj;
+}
+
+// Two nodes' reference-order scores (node j0 in .x, j1 in .y) of the
+// lane's Q cells from their packed counts, then the selection, j0 first.
+template <int Q, int NW>
+__device__ __forceinline__ void max_update2(const uint32_t (&k0)[NW], int j0,
+                                            const uint32_t (&k1)[NW], int j1,
+                                            const float2 (&pdb)[Q],
+                                            const float2 (&pmb)[Q],
+                                            const LogTable2 &L2,
+                                            float (&best)[Q], int (&bj)[Q]) {
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    const float s = pair_score_b(__int_as_float(0x4B000000 | (k[q] & 0xFFu)),
-                                 __int_as_float(0x4B000000 | (k[q] >> 8)),
-                                 pdb[q], pmb[q], L.l00, L.l01, L.l10, L.l11);
-    const bool up = s > best[q] || (s == best[q] && j < bj[q]);
-    best[q] = up ? s : best[q];
-    bj[q] = up ? j : bj[q];
+    const float2 db = make_float2(pack_d_biased(k0[q >> 1], q),
+                                  pack_d_biased(k1[q >> 1], q));
+    const float2 mb = make_float2(pack_m_biased(k0[q >> 1], q),
+                                  pack_m_biased(k1[q >> 1], q));
+    const float2 s = pair_score_b2(db, mb, pdb[q], pmb[q], L2);
+    max_select(s.x, j0, best[q], bj[q]);
+    max_select(s.y, j1, best[q], bj[q]);
   }
 }
 
 template <int W32, int Q>
 __device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb,
-                                                  const LogTable &L, int c0,
-                                                  int stride, int lane,
-                                                  const SumCtx &sx, int &k,
-                                                  int &m) {
+                                                  const LogTable &L, float nz,
+                                                  int lane, const SumCtx &sx,
+                                                  int &k, int &m) {
+  constexpr int NW = kPackWords<Q>;
+  const LogTable2 L2 = log_table2(L, nz);
   float best[Q];
   int bj[Q];
+  float2 pdb[Q], pmb[Q];
   {
     const int root = (int)(sx.ord[0] & 0xFF);
+    uint32_t zero[NW];
+#pragma unroll
+    for (int w = 0; w < NW; w++) zero[w] = 0u;
+    st_pack<Q>(sx.cnt, root * 32 + lane, zero);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      sx.cnt[(root * Q + q) * 32 + lane] = 0;
       best[q] = pair_score(0, 0, cb.pdb[q], cb.pmb[q], L.l00, L.l01, L.l10,
                            L.l11);
       bj[q] = root;
+      pdb[q] = dup2(cb.pdb[q]);
+      pmb[q] = dup2(cb.pmb[q]);
     }
   }
   int i = 1;
   if (i + 1 < n) {
-    uint32_t kA[Q], kB[Q], kA1[Q], kB1[Q];
+    uint32_t kA0[NW], kA1[NW], kB0[NW], kB1[NW];
     int jA0, jA1, jB0, jB1;
-    inherit_pair<Q>(sx, i, c0, stride, lane, kA, kA1, jA0, jA1);
+    inherit_pair<Q>(sx, i, lane, kA0, kA1, jA0, jA1);
 #pragma unroll 1
     for (; i + 5 < n; i += 4) {
-      inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
-      max_update<Q>(kA, jA0, cb.pdb, cb.pmb, L, best, bj);
-      max_update<Q>(kA1, jA1, cb.pdb, cb.pmb, L, best, bj);
-      inherit_pair<Q>(sx, i + 4, c0, stride, lane, kA, kA1, jA0, jA1);
-      max_update<Q>(kB, jB0, cb.pdb, cb.pmb, L, best, bj);
-      max_update<Q>(kB1, jB1, cb.pdb, cb.pmb, L, best, bj);
+      inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+      max_update2<Q, NW>(kA0, jA0, kA1, jA1, pdb, pmb, L2, best, bj);
+      inherit_pair<Q>(sx, i + 4, lane, kA0, kA1, jA0, jA1);
+      max_update2<Q, NW>(kB0, jB0, kB1, jB1, pdb, pmb, L2, best, bj);
     }
     if (i + 3 < n) {
-      inherit_pair<Q>(sx, i + 2, c0, stride, lane, kB, kB1, jB0, jB1);
-      max_update<Q>(kA, jA0, cb.pdb, cb.pmb, L, best, bj);
-      max_update<Q>(kA1, jA1, cb.pdb, cb.pmb, L, best, bj);
-      max_update<Q>(kB, jB0, cb.pdb, cb.pmb, L, best, bj);
-      max_update<Q>(kB1, jB1, cb.pdb, cb.pmb, L, best, bj);
+      inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+      max_update2<Q, NW>(kA0, jA0, kA1, jA1, pdb, pmb, L2, best, bj);
+      max_update2<Q, NW>(kB0, jB0, kB1, jB1, pdb, pmb, L2, best, bj);
       i += 4;
     } else {
-      max_update<Q>(kA, jA0, cb.pdb, cb.pmb, L, best, bj);
-      max_update<Q>(kA1, jA1, cb.pdb, cb.pmb, L, best, bj);
+      max_update2<Q, NW>(kA0, jA0, kA1, jA1, pdb, pmb, L2, best, bj);
       i += 2;
     }
   }
   if (i < n) {
-    const uint32_t o = sx.ord[i];
-    const int j = (int)(o & 0xFF), p = (int)(o >> 8);
-    uint32_t kk[Q];
+    uint32_t kk[NW];
+    int j;
+    inherit_one<Q>(sx, i, lane, kk, j);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
-      kk[q] = (uint32_t)sx.cnt[(p * Q + q) * 32 + lane] +
-              gene_increment(sx, j, c0 + stride * q + lane);
-      sx.cnt[(j * Q + q) * 32 + lane] = (uint16_t)kk[q];
+      const float s = pair_score_b(pack_d_biased(kk[q >> 1], q),
+                                   pack_m_biased(kk[q >> 1], q), cb.pdb[q],
+                                   cb.pmb[q], L.l00, L.l01, L.l10, L.l11);
+      max_select(s, j, best[q], bj[q]);
     }
-    max_update<Q>(kk, j, cb.pdb, cb.pmb, L, best, bj);
   }
   // the counts at the chosen nodes: k = popc(K & A) = d + m
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    const uint32_t c = sx.cnt[(bj[q] * Q + q) * 32 + lane];
-    k += (int)(c & 0xFFu) + (int)(c >> 8);
-    m += (int)(c >> 8);
+    uint32_t c[NW];
+    ld_pack<Q>(sx.cnt, bj[q] * 32 + lane, c);
+    const uint32_t f = pack_field<NW>(c, q);
+    k += (int)(f & 0xFFu) + (int)(f >> 8);
+    m += (int)(f >> 8);
   }
 }
 
@@ -1304,21 +1502,21 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
   int k = 0, m = 0, bj[Q];
   bool inherit = false;
   if constexpr (W32 <= 4)
-    inherit = resident && sx.cnt != nullptr && sx.inc != nullptr &&
+    inherit = resident && sx.cnt.w != nullptr && sx.inc.w != nullptr &&
               sx.par != nullptr;
   if (inherit) {
     if constexpr (W32 <= 4) {
       canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
-      max_cells_inherit<W32, Q>(n, cb, L, 32 * wic, 32 * wpc, lane, sx, k, m);
+      max_cells_inherit<W32, Q>(n, cb, L, ds.neg_zero, lane, sx, k, m);
     }
   } else if (resident) {
-    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
+    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, ds.neg_zero, bj);
     counts_at<W32, Q>(rows, cb, bj, k, m);
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
+      best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, ds.neg_zero, bj);
       counts_at<W32, Q>(rows, cb, bj, k, m);
     }
   }

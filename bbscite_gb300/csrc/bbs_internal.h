@@ -21,6 +21,14 @@ __host__ __device__ constexpr int rs_of_w32(int w32) {
   return 2 * ((w32 + 1) / 2);
 }
 __host__ __device__ constexpr int w32_of_nodes(int n) { return (n + 31) / 32; }
+// Chains inherit counts from the parent (max or sum score) when their rows
+// have up to four words and all their cells stay in registers (at most
+// cells_per_pass = 32 x cells per lane x warps per chain): the increment
+// tables and each warp's count table exist then.
+__host__ __device__ constexpr bool inherits_counts(int w32, int n_cells,
+                                                   int cells_per_pass) {
+  return w32 <= 4 && n_cells <= cells_per_pass;
+}
 
 // Cumulative move thresholds and jump sd (src/RawMoveDistribution.hpp:
 // 119-131, src/Parameters.hpp:451-584).  The first threshold is the
@@ -39,6 +47,11 @@ struct DatasetDev {
                       // (src/TreeScorer.hpp:99-106)
   float bpa, bpb;     // Beta prior parameters (src/TreeScorer.hpp:108-111)
   float lg_ab, lg_a, lg_b;  // log(tgamma(a+b)), log(tgamma(a)), log(tgamma(b))
+  float neg_zero;     // -0.0f.  Paired products are taken as fused
+                      // multiply-adds of this addend: read from memory, it
+                      // cannot be folded, so the compiler cannot contract a
+                      // product with the sum that follows it (it does so for
+                      // a paired multiply, whatever its rounding modifier)
 };
 
 // The sampling rules of one dataset's chains.
@@ -106,8 +119,11 @@ struct BatchArgs {
   const volatile int *cancel;
   int *status;
   int max_nodes;             // shared memory is sized for this
-  int table_ds;              // the launch's only dataset (sum score:
-                             // inherited counts), or -1
+  int table_ds;              // the launch's only dataset, or -1
+  int with_counts;           // 1: the chains inherit counts (rows of up to
+                             // four words, one dataset whose cells stay in
+                             // registers); shared memory holds the count
+                             // and increment tables only then
 };
 
 // Initial state of each chain: evaluate its tree at (alpha_mean,

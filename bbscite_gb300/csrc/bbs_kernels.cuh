@@ -43,75 +43,93 @@ __device__ __forceinline__ void copy_rows(const uint32_t *src, uint32_t *dst,
 // Shared memory of the chain kernels, in bytes (16-byte aligned pieces).
 __host__ __device__ inline int align16(int b) { return (b + 15) & ~15; }
 
-// Per warp of a sum-score chain: the canonical node order, its depth
-// histogram and (rows of up to four words) the packed counts of every node
-// for the lane's cells.
-__host__ __device__ inline int sum_warp_bytes(int n, int w32, int q) {
+// Per warp of a chain with the node-order scratch (every sum-score chain:
+// its order is canonical; every chain that inherits counts): the canonical
+// node order, its depth histogram and, with `counts`, the packed counts of
+// every node for the lane's cells (2 q bytes per node and lane).
+__host__ __device__ inline int sum_warp_bytes(int n, int w32, int q,
+                                              bool counts) {
   return align16(2 * n) + align16(4 * 32 * ((n + 31) / 32)) +
-         (w32 <= 4 ? align16(2 * n * q * 32) : 0);
+         (counts && w32 <= 4 ? align16(2 * q * n * 32) : 0);
 }
 
 // One chain slot: two row buffers, the partial sums of both step parities
-// (2 x wpc x 12 words) and a flag word; for the sum score, the current and
-// proposed parent vectors and each warp's sum scratch.
-__host__ __device__ inline int slot_bytes(int n, int rs, int wpc, bool sum,
-                                          int w32, int q) {
+// (2 x wpc x 12 words) and a flag word; with the scratch, the current and
+// proposed parent vectors and each warp's scratch.
+__host__ __device__ inline int slot_bytes(int n, int rs, int wpc, bool scratch,
+                                          int w32, int q, bool counts) {
   int b = 4 * (2 * n * rs + 24 * wpc + 4);
-  if (sum) b += align16(2 * n) + wpc * sum_warp_bytes(n, w32, q);
+  if (scratch) b += align16(2 * n) + wpc * sum_warp_bytes(n, w32, q, counts);
   return b;
 }
 
-// Kernels with the node-order scratch: every sum-score kernel (its order
-// is canonical) and every kernel with rows of up to four words (inherited
-// counts, max or sum score).
-template <int W32, bool SUM>
-inline constexpr bool kScratch = SUM || W32 <= 4;
-
-// After the slots: the block's table of per-gene increments (rows of up to
-// four words) for its 32 * q * wpc resident cell slots.
+// After the slots, with `counts`: the block's tables of per-gene
+// increments, one per warp part of a chain (wpc), each for that warp's
+// 32 q cell slots.
+__host__ __device__ inline int inc_table_bytes(int n, int q) {
+  return align16(2 * q * n * 32);
+}
 __host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
-                                           bool sum) {
-  return sum && w32 <= 4 ? align16(2 * n * 32 * q * wpc) : 0;
+                                           bool counts) {
+  return counts && w32 <= 4 ? wpc * inc_table_bytes(n, q) : 0;
 }
 
-// The sum-score pieces of a slot: parent vectors and warp wic's scratch.
+// The scratch pieces of a slot: parent vectors and warp wic's scratch.
 // (Host-callable too: the layout test walks it over every shape.)
 struct SlotSum {
   uint8_t *par0, *par1;
   SumCtx sx;
 };
 
-__host__ __device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n, int rs,
-                                            int wpc, int wic, int w32, int q) {
+__host__ __device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n,
+                                                     int rs, int wpc, int wic,
+                                                     int w32, int q,
+                                                     bool counts) {
   SlotSum o{};
   uint8_t *p = slot + 4 * (2 * n * rs + 24 * wpc + 4);
   o.par0 = p;
   o.par1 = p + n;
-  p += align16(2 * n) + wic * sum_warp_bytes(n, w32, q);
+  p += align16(2 * n) + wic * sum_warp_bytes(n, w32, q, counts);
   o.sx.ord = reinterpret_cast<uint16_t *>(p);
   p += align16(2 * n);
   o.sx.hist = reinterpret_cast<int *>(p);
   p += align16(4 * 32 * ((n + 31) / 32));
-  o.sx.cnt = w32 <= 4 ? reinterpret_cast<uint16_t *>(p) : nullptr;
+  if (counts && w32 <= 4) o.sx.cnt = pack_table<CountTable>(p, n, q);
   return o;
 }
 
-// The block's increment table: gene j of cell slot c (cell c of the
-// dataset; zero past its cells) is D | M << 8 of that gene.  Cell rows are
-// read with the stride rs that load_cells uses.
-__device__ __forceinline__ void build_increments(uint16_t *table, int stride,
+// The block's increment tables: for warp part wic of wpc and lane l, the
+// cells c = 32 wic + 32 wpc q + l (q < Q; zero past the dataset's cells),
+// as load_cells takes them; gene j's entry packs D bit | M bit << 8 of each
+// such cell as the count table packs counts.  Cell rows are read with the
+// stride rs that load_cells uses.
+template <int Q>
+__device__ __forceinline__ void build_increments(uint8_t *table, int wpc,
                                                  const DatasetDev &ds, int rs) {
+  constexpr int NW = kPackWords<Q>;
   const int n = ds.n_nodes;
-  for (int idx = threadIdx.x; idx < n * stride; idx += blockDim.x) {
-    const int j = idx / stride, c = idx - j * stride;
-    uint32_t v = 0;
-    if (c < ds.n_cells) {
-      const uint32_t k = __ldg(ds.K + (size_t)c * rs + (j >> 5));
-      const uint32_t m = __ldg(ds.M + (size_t)c * rs + (j >> 5));
-      const uint32_t b = 1u << (j & 31);
-      v = ((k & ~m & b) ? 1u : 0u) | ((m & b) ? 256u : 0u);
+  for (int idx = threadIdx.x; idx < wpc * n * 32; idx += blockDim.x) {
+    const int wic = idx / (n * 32);
+    const int rem = idx - wic * n * 32;
+    const int j = rem >> 5, l = rem & 31;
+    uint32_t k[NW];
+#pragma unroll
+    for (int w = 0; w < NW; w++) k[w] = 0u;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const int c = 32 * wic + 32 * wpc * q + l;
+      uint32_t v = 0;
+      if (c < ds.n_cells) {
+        const uint32_t kw = __ldg(ds.K + (size_t)c * rs + (j >> 5));
+        const uint32_t mw = __ldg(ds.M + (size_t)c * rs + (j >> 5));
+        const uint32_t bit = 1u << (j & 31);
+        v = ((kw & ~mw & bit) ? 1u : 0u) | ((mw & bit) ? 256u : 0u);
+      }
+      k[q >> 1] |= v << (16 * (q & 1));
     }
-    table[idx] = (uint16_t)v;
+    const CountTable t =
+        pack_table<CountTable>(table + (size_t)wic * inc_table_bytes(n, Q), n, Q);
+    st_pack<Q>(t, j * 32 + l, k);
   }
 }
 
@@ -201,7 +219,7 @@ __device__ __forceinline__ void run_chain(
   uint8_t *cpar = nullptr, *ppar = nullptr;
   bool cur_par_ok = false;  // cpar describes cur
   if constexpr (W32 <= 4) {
-    if (ss.sx.inc != nullptr && resident) {
+    if (ss.sx.inc.w != nullptr && resident) {
       cpar = ss.par0;
       ppar = ss.par1;
       if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
@@ -483,26 +501,28 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   const int cpb = wpb / wpc;
   const int slot = wib / wpc, wic = wib - slot * wpc;
   const int n = a.ds.n_nodes;
-  const int sb = slot_bytes(n, RS, wpc, kScratch<W32, SUM>, W32, Q);
+  const bool resident = a.ds.n_cells <= 32 * wpc * Q;
+  // the same decisions as the launcher's, for the whole block
+  const bool counts = inherits_counts(W32, a.ds.n_cells, 32 * wpc * Q);
+  const bool scratch = SUM || counts;
+  const int sb = slot_bytes(n, RS, wpc, scratch, W32, Q, counts);
   uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)slot * sb;
   uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   uint32_t *buf1 = buf0 + n * RS;
   int *part = reinterpret_cast<int *>(buf0 + 2 * n * RS);
   volatile int *sflag = part + 24 * wpc;
-  const bool resident = a.ds.n_cells <= 32 * wpc * Q;
   Cells<W32, Q> cb;
   if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
   SlotSum ss{};
-  if constexpr (kScratch<W32, SUM>) {
-    ss = slot_sum(slot_base, n, RS, wpc, wic, W32, Q);
+  if (scratch) {
+    ss = slot_sum(slot_base, n, RS, wpc, wic, W32, Q, counts);
     if constexpr (W32 <= 4) {
-      if (resident) {  // the same for the whole block
-        uint16_t *table = reinterpret_cast<uint16_t *>(
-            reinterpret_cast<uint8_t *>(smem) + (size_t)cpb * sb);
-        build_increments(table, 32 * Q * wpc, a.ds, RS);
+      if (counts) {
+        uint8_t *table = reinterpret_cast<uint8_t *>(smem) + (size_t)cpb * sb;
+        build_increments<Q>(table, wpc, a.ds, RS);
         __syncthreads();
-        ss.sx.inc = table;
-        ss.sx.inc_stride = 32 * Q * wpc;
+        ss.sx.inc = pack_table<IncTable>(
+            table + (size_t)wic * inc_table_bytes(n, Q), n, Q);
       }
     }
   }
@@ -546,7 +566,7 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
   const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
   // the increment table holds the cells of dataset b.table_ds only
   SlotSum ss = ss_in;
-  if ((int)d != b.table_ds) ss.sx.inc = nullptr;
+  if ((int)d != b.table_ds) ss.sx.inc = IncTable{nullptr, nullptr};
   run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
                          nullptr, nullptr, 1, b.states + chain, nullptr,
                          nullptr, b.n_steps, b.cancel, b.status, buf0, buf1,
@@ -562,24 +582,25 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
   constexpr int RS = rs_of_w32(W32);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int sb = slot_bytes(b.max_nodes, RS, 1, kScratch<W32, SUM>, W32, Q);
+  // one dataset in this launch with its cells in registers: inherited
+  // counts (the host's decision, the same in every thread)
+  const bool counts = b.with_counts != 0;
+  const bool scratch = SUM || counts;
+  const int sb = slot_bytes(b.max_nodes, RS, 1, scratch, W32, Q, counts);
   uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)wib * sb;
   uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
   volatile int *sflag = part + 24;
   SlotSum ss{};
-  if constexpr (kScratch<W32, SUM>) {
-    ss = slot_sum(slot_base, b.max_nodes, RS, 1, 0, W32, Q);
+  if (scratch) {
+    ss = slot_sum(slot_base, b.max_nodes, RS, 1, 0, W32, Q, counts);
     if constexpr (W32 <= 4) {
-      // one dataset in this launch with its cells in registers: the block's
-      // increment table (the same decision in every thread of the block)
-      if (b.table_ds >= 0 && b.ds[b.table_ds].n_cells <= 32 * Q) {
-        uint16_t *table = reinterpret_cast<uint16_t *>(
-            reinterpret_cast<uint8_t *>(smem) + (size_t)(blockDim.x >> 5) * sb);
-        build_increments(table, 32 * Q, b.ds[b.table_ds], RS);
+      if (counts) {
+        uint8_t *table = reinterpret_cast<uint8_t *>(smem) +
+                         (size_t)(blockDim.x >> 5) * sb;
+        build_increments<Q>(table, 1, b.ds[b.table_ds], RS);
         __syncthreads();
-        ss.sx.inc = table;
-        ss.sx.inc_stride = 32 * Q;
+        ss.sx.inc = pack_table<IncTable>(table, b.ds[b.table_ds].n_nodes, Q);
       }
     }
   }
@@ -699,7 +720,8 @@ __global__ void __launch_bounds__(128) score_kernel(const ScoreArgs a) {
   for (int c0 = 0; c0 < a.ds.n_cells; c0 += 32 * Q) {
     load_cells<W32, Q>(cb, a.ds, c0, 32, lane);
     int bj[Q];
-    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, bj);
+    best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, a.ds.neg_zero,
+                          bj);
     counts_at<W32, Q>(rows, cb, bj, k, m);
     if constexpr (ATTACH) {
 #pragma unroll

@@ -24,9 +24,11 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   if (a.wpc > 1) cpb = 1;
   const int threads = 32 * a.wpc * cpb;
   if (threads > 128) return (int)cudaErrorInvalidConfiguration;
+  const bool counts = inherits_counts(W32, a.ds.n_cells, 32 * a.wpc * Q);
   const size_t smem =
-      (size_t)cpb * slot_bytes(a.ds.n_nodes, RS, a.wpc, kScratch<W32, SUM>, W32, Q) +
-      table_bytes(a.ds.n_nodes, W32, Q, a.wpc, kScratch<W32, SUM>);
+      (size_t)cpb * slot_bytes(a.ds.n_nodes, RS, a.wpc, SUM || counts, W32, Q,
+                               counts) +
+      table_bytes(a.ds.n_nodes, W32, Q, a.wpc, counts);
   auto kern = mcmc_kernel<W32, Q, SUM, REC>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
@@ -46,9 +48,13 @@ template <int W32, int Q, bool SUM>
 int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   const int threads = 32 * wpb;
+  const bool counts = b.with_counts != 0;
+  if (counts && (W32 > 4 || b.table_ds < 0))
+    return (int)cudaErrorInvalidValue;  // counts need one dataset's rows
   const size_t smem =
-      (size_t)wpb * slot_bytes(b.max_nodes, RS, 1, kScratch<W32, SUM>, W32, Q) +
-      (b.table_ds >= 0 ? table_bytes(b.max_nodes, W32, Q, 1, kScratch<W32, SUM>) : 0);
+      (size_t)wpb * slot_bytes(b.max_nodes, RS, 1, SUM || counts, W32, Q,
+                               counts) +
+      table_bytes(b.max_nodes, W32, Q, 1, counts);
   auto kern = batch_kernel<W32, Q, SUM>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;

@@ -3,10 +3,12 @@
 // 1..4 warps per chain (one-warp chains 1..4 per block), both scores.  For
 // each chain slot the pieces the kernels address -- the two row buffers,
 // both parities of the per-warp partial sums, the flag word, the parent
-// vectors, and each warp's node order, depth histogram and count table --
-// must lie inside the slot, be disjoint and be aligned for their element
-// type; the block's increment table must lie after the slots and inside the
-// launch's dynamic shared memory.  Prints "layout ok <cases>" or the first
+// vectors, and each warp's node order, depth histogram and count table
+// (its full words and, for an odd number of cells per lane, its 16-bit
+// fields) -- must lie inside the slot, be disjoint and be aligned for their
+// element type; the block's increment tables (one per warp of a chain,
+// split the same way) must lie after the slots and inside the launch's
+// dynamic shared memory.  Prints "layout ok <cases>" or the first
 // violation (exit status 1).
 #include <cstdint>
 #include <cstdio>
@@ -31,16 +33,27 @@ bool fail(const char *what, int n, int q, int wpc, int cpb, bool sum,
   return false;
 }
 
-// One launch: cpb slots of wpc warps, the table after them.  `table` says
-// whether the launch builds an increment table (plain kernel: always with
-// the scratch; batched kernel: when a launch group holds one dataset).
-bool check(int n, int q, int wpc, int cpb, bool sum, bool table) {
+// A packed table of n nodes x 32 lanes for q cells per lane: q/2 words per
+// entry (one 32- or 64-bit access) at w, the odd cell's 16-bit fields at h.
+void add_table(std::vector<Piece> &all, const char *name, size_t w, size_t h,
+               int n, int q) {
+  const int np = q / 2;
+  if (np > 0)
+    all.push_back({name, w, w + (size_t)4 * np * n * 32, (size_t)4 * np});
+  if (q & 1) all.push_back({name, h, h + (size_t)2 * n * 32, 2});
+}
+
+// One launch: cpb slots of wpc warps, the tables after them.  `counts`
+// says whether the chains inherit counts (rows of up to four words, cells
+// in registers): the slots then carry count tables and the launch its
+// increment tables.
+bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
   const int w32 = bbs::w32_of_nodes(n);
   const int rs = bbs::rs_of_w32(w32);
-  const bool scratch = sum || w32 <= 4;  // kScratch<W32, SUM>
-  const int sb = bbs::slot_bytes(n, rs, wpc, scratch, w32, q);
-  const size_t tb =
-      table ? (size_t)bbs::table_bytes(n, w32, q, wpc, scratch) : 0;
+  if (w32 > 4) counts = false;
+  const bool scratch = sum || counts;
+  const int sb = bbs::slot_bytes(n, rs, wpc, scratch, w32, q, counts);
+  const size_t tb = (size_t)bbs::table_bytes(n, w32, q, wpc, counts);
   const size_t total = (size_t)cpb * sb + tb;
   std::vector<uint8_t> smem(total + 16);
   uint8_t *base = smem.data();
@@ -64,7 +77,7 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool table) {
     if (scratch) {
       for (int wic = 0; wic < wpc; wic++) {
         const bbs::SlotSum ss =
-            bbs::slot_sum(base + o, n, rs, wpc, wic, w32, q);
+            bbs::slot_sum(base + o, n, rs, wpc, wic, w32, q, counts);
         auto off = [&](const void *p) {
           return (size_t)(static_cast<const uint8_t *>(p) - base);
         };
@@ -79,13 +92,13 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool table) {
         if (hist < (size_t)4 * n)
           return fail("histogram smaller than n ints", n, q, wpc, cpb, sum, "");
         all.push_back({"hist", off(ss.sx.hist), off(ss.sx.hist) + hist, 4});
-        if (w32 <= 4) {
-          if (ss.sx.cnt == nullptr)
+        if (counts) {
+          if (ss.sx.cnt.w == nullptr)
             return fail("no count table", n, q, wpc, cpb, sum, "");
-          all.push_back({"cnt", off(ss.sx.cnt),
-                         off(ss.sx.cnt) + (size_t)2 * n * q * 32, 2});
-        } else if (ss.sx.cnt != nullptr) {
-          return fail("count table for wide rows", n, q, wpc, cpb, sum, "");
+          add_table(all, "cnt", off(ss.sx.cnt.w), off(ss.sx.cnt.h), n, q);
+        } else if (ss.sx.cnt.w != nullptr) {
+          return fail("count table without inherited counts", n, q, wpc,
+                      cpb, sum, "");
         }
       }
     }
@@ -93,12 +106,18 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool table) {
       if (all[i].lo < o || all[i].hi > o + sb)
         return fail("piece outside its slot", n, q, wpc, cpb, sum, all[i].name);
   }
-  if (table && scratch && w32 <= 4) {
+  if (counts) {
     const size_t lo = (size_t)cpb * sb;
-    const size_t need = (size_t)2 * n * 32 * q * wpc;
-    if (tb < need)
-      return fail("increment table too small", n, q, wpc, cpb, sum, "");
-    all.push_back({"table", lo, lo + need, 16});
+    if (tb != (size_t)wpc * bbs::inc_table_bytes(n, q))
+      return fail("increment tables sized wrongly", n, q, wpc, cpb, sum, "");
+    for (int wic = 0; wic < wpc; wic++) {
+      uint8_t *t = base + lo + (size_t)wic * bbs::inc_table_bytes(n, q);
+      const bbs::IncTable it = bbs::pack_table<bbs::IncTable>(t, n, q);
+      add_table(all, "inc",
+                (size_t)(reinterpret_cast<const uint8_t *>(it.w) - base),
+                (size_t)(reinterpret_cast<const uint8_t *>(it.h) - base), n,
+                q);
+    }
   }
   for (size_t i = 0; i < all.size(); i++) {
     if (all[i].hi > total)
@@ -120,18 +139,17 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool table) {
 int main() {
   for (int n = 2; n <= 256; n++)
     for (int q = 1; q <= bbs::kMaxQ; q++)
-      for (int sum = 0; sum < 2; sum++) {
-        // plain kernel: one-warp chains 1..4 per block, or one chain of
-        // 2..4 warps; its table whenever the slots carry the scratch
-        for (int cpb = 1; cpb <= 4; cpb++)
-          if (!check(n, q, 1, cpb, sum != 0, true)) return 1;
-        for (int wpc = 2; wpc <= 4; wpc++)
-          if (!check(n, q, wpc, 1, sum != 0, true)) return 1;
-        // batched kernel: one-warp slots, with or without the table
-        for (int wpb = 1; wpb <= 4; wpb++)
-          for (int table = 0; table < 2; table++)
-            if (!check(n, q, 1, wpb, sum != 0, table != 0)) return 1;
-      }
+      for (int sum = 0; sum < 2; sum++)
+        for (int counts = 0; counts < 2; counts++) {
+          // plain kernel: one-warp chains 1..4 per block, or one chain of
+          // 2..4 warps
+          for (int cpb = 1; cpb <= 4; cpb++)
+            if (!check(n, q, 1, cpb, sum != 0, counts != 0)) return 1;
+          for (int wpc = 2; wpc <= 4; wpc++)
+            if (!check(n, q, wpc, 1, sum != 0, counts != 0)) return 1;
+        }
+  // (the batched kernel's launches are one-warp slots, 1..4 per block: the
+  // cases of the plain kernel with wpc = 1)
   std::printf("layout ok %ld\n", g_cases);
   return 0;
 }

@@ -140,9 +140,9 @@ def test_shared_memory_layout_of_every_launch_shape(tmp_path):
     """tests/cpp/layout_probe.cu walks the chain kernels' shared-memory
     layout (the slot and table sizes and the per-warp pieces the kernels
     address) over every node count, cells per lane, warps per chain and
-    chains per block that the launchers accept: every piece lies inside its
-    slot, the pieces are disjoint and aligned, and the increment table fits
-    after the slots."""
+    chains per block that the launchers accept, with and without inherited
+    counts: every piece lies inside its slot, the pieces are disjoint and
+    aligned, and the increment tables fit after the slots."""
     import subprocess
     from bbscite_gb300 import build as B
     exe = str(tmp_path / "layout_probe")
@@ -153,7 +153,7 @@ def test_shared_memory_layout_of_every_launch_shape(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
     assert r.stdout.startswith("layout ok "), r.stdout
-    assert int(r.stdout.split()[2]) == 255 * 4 * 2 * 15
+    assert int(r.stdout.split()[2]) == 255 * 4 * 2 * 2 * 7
 
 
 def _ctype_of(decl: str):
