@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "bbs_internal.h"
+#include "bbs_layout.h"
 
 using namespace bbs;
 
@@ -222,6 +223,7 @@ int put_string(const std::string &s, char *buf, size_t cap, size_t *len) {
 // ------------------------------------------------------------------------
 struct bbs_ctx {
   int device = 0, n_sms = 0;
+  int smem_sm = 0, smem_block = 0, smem_reserved = 0;  // per SM / block
   cudaStream_t stream = nullptr;
   uint32_t n_cells = 0, n_genes = 0, n_nodes = 0, W64 = 0, RS = 0;
   bbs_params params{};
@@ -746,6 +748,12 @@ int bbs_create(bbs_ctx **out, const uint64_t *is_mutated,
     c->RS = 2 * c->W64;
     cudaGetDevice(&c->device);
     cudaDeviceGetAttribute(&c->n_sms, cudaDevAttrMultiProcessorCount, c->device);
+    cudaDeviceGetAttribute(&c->smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor,
+                           c->device);
+    cudaDeviceGetAttribute(&c->smem_block, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                           c->device);
+    cudaDeviceGetAttribute(&c->smem_reserved, cudaDevAttrReservedSharedMemoryPerBlock,
+                           c->device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     HostDataset h;
     prepare_dataset(params, n_cells, n_genes, is_mutated, is_known, h);
@@ -817,6 +825,24 @@ int bbs_get_sizes(const bbs_ctx *c, uint32_t *n_cells, uint32_t *n_genes,
 
 namespace {
 
+// One-warp chains per block (1-8; they share the block's increment table)
+// that keep the most warps resident on an SM; ties keep the smaller block.
+int pick_chains_per_block(const bbs_ctx *c, int q) {
+  const bool sum = c->md.score_mode != 0;
+  int best = 1, best_warps = 0;
+  for (int cpb = 1; cpb * 32 <= chain_max_threads(q); cpb++) {
+    const int smem = chain_launch_smem((int)c->n_nodes, (int)c->n_cells, q, 1,
+                                       cpb, sum);
+    const int w = chain_resident_warps(smem, cpb, q, c->smem_sm, c->smem_block,
+                                       c->smem_reserved);
+    if (w > best_warps) {
+      best_warps = w;
+      best = cpb;
+    }
+  }
+  return best;
+}
+
 // Launch shape without timing: split the cells over up to four warps per
 // chain when there are too few chains to give every scheduler ~3 warps,
 // preferring shapes that leave no cell slots empty.
@@ -841,9 +867,7 @@ void default_launch(bbs_ctx *c) {
     c->wpc = 4;
     c->q = qmax;
   }
-  // four one-warp chains per block share the block's increment table, and
-  // two such blocks fit an SM's shared memory
-  c->cpb = c->wpc == 1 ? 4 : 1;
+  c->cpb = c->wpc == 1 ? pick_chains_per_block(c, c->q) : 1;
 }
 
 size_t tree_words(const bbs_ctx *c, uint32_t n_trees) {
@@ -1038,8 +1062,9 @@ int bbs_set_launch(bbs_ctx *c, int cells_per_lane, int warps_per_chain,
     return fail(BBS_ERR_INPUT, "cells per lane must be in [1, %d]", qmax);
   if (warps_per_chain < 0 || warps_per_chain > 4)
     return fail(BBS_ERR_INPUT, "warps per chain must be in [1, 4]");
-  if (chains_per_block < 0 || chains_per_block > 4)
-    return fail(BBS_ERR_INPUT, "chains per block must be in [1, 4]");
+  if (chains_per_block < 0 || 32 * chains_per_block > kMaxBlockThreads)
+    return fail(BBS_ERR_INPUT, "chains per block must be in [1, %d]",
+                kMaxBlockThreads / 32);
   if (cells_per_lane) c->q = cells_per_lane;
   if (warps_per_chain) c->wpc = warps_per_chain;
   if (chains_per_block) c->cpb = chains_per_block;
@@ -1092,8 +1117,9 @@ int bbs_autotune(bbs_ctx *c, uint32_t probe_steps, float *best_ms) {
     for (int wpc = 1; wpc <= 4; wpc++)
       for (int q = 1; q <= qmax; q++) {
         if (wpc * q > groups + 1) continue;  // mostly empty cell slots
-        for (int cpb : {1, 2, 4}) {
+        for (int cpb : {1, 2, 4, 7, 8}) {
           if (wpc > 1 && cpb > 1) continue;
+          if (32 * cpb > chain_max_threads(q)) continue;
           c->q = q;
           c->wpc = wpc;
           c->cpb = cpb;
@@ -2167,7 +2193,9 @@ int bbs_batch_set_launch(bbs_batch *b, int q, int wpb, int merge) {
   if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
   if (q < 0 || q > 4)
     return fail(BBS_ERR_INPUT, "cells per lane must be 1, 2, 3 or 4");
-  if (wpb < 0 || wpb > 4) return fail(BBS_ERR_INPUT, "warps per block must be in [1, 4]");
+  if (wpb < 0 || 32 * wpb > kMaxBlockThreads)
+    return fail(BBS_ERR_INPUT, "warps per block must be in [1, %d]",
+                kMaxBlockThreads / 32);
   if (q) b->q = q;
   if (wpb) b->wpb = wpb;
   if (merge >= 0 && merge != b->merge) {
@@ -2211,7 +2239,8 @@ int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
     int bq = b->q, bw = b->wpb, bm = b->merge;
     for (int merge : {0, 1})
       for (int q : {1, 2, 3, 4})
-        for (int wpb : {1, 2, 4}) {
+        for (int wpb : {1, 2, 4, 7, 8}) {
+          if (32 * wpb > chain_max_threads(q)) continue;
           int r = bbs_batch_set_launch(b, q, wpb, merge);
           if (r != BBS_OK) return r;
           BBS_CUDA(cudaEventRecord(b->ev0, b->stream), "event");

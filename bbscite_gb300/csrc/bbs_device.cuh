@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "bbs_internal.h"
+#include "bbs_layout.h"
 
 namespace bbs {
 
@@ -451,60 +452,36 @@ __device__ __forceinline__ float2 dup2(float x) { return make_float2(x, x); }
 // ------------------------------------------------------------------------
 // Packed counts.  A lane's Q cells' counts of one node, d | m << 8 per cell
 // (d, m <= 255: a count of genes), two cells per 32-bit word: NW = (Q+1)/2
-// register words, word q/2 holding cell q in bits 16 (q & 1) upwards.
-// Adding two packed words adds every field at once (no field can carry
-// into the next).  A field becomes the exact biased float 2^23 + count
-// with one byte permute into the bit pattern 0x4B0000xx.  In shared memory
-// a table of entries [node][lane] keeps the Q/2 full words of an entry
-// together (one 32- or 64-bit access) and, for odd Q, the last cell's
-// field in a 16-bit table of its own: 2 Q bytes per entry.
+// words, word q/2 holding cell q in bits 16 (q & 1) upwards.  Adding two
+// packed words adds every field at once (no field can carry into the
+// next).  A field becomes the exact biased float 2^23 + count with one byte
+// permute into the bit pattern 0x4B0000xx.  In shared memory a table of
+// entries [node][lane] keeps an entry's NW words together: one 32- or
+// 64-bit access per entry (for three cells the fourth field is unused).
 // ------------------------------------------------------------------------
 template <int Q>
 inline constexpr int kPackWords = (Q + 1) / 2;
 
-// A count table: full words at w, the odd cell's fields at h.
-template <typename W, typename H>
-struct PackTable {
-  W *w;
-  H *h;
-};
-using CountTable = PackTable<uint32_t, uint16_t>;
-using IncTable = PackTable<const uint32_t, const uint16_t>;
-
-// Table pointers for n nodes at `base` (2 Q n 32 bytes).
-template <typename T>
-__host__ __device__ inline T pack_table(void *base, int n, int q) {
-  T t;
-  t.w = reinterpret_cast<decltype(t.w)>(base);
-  t.h = reinterpret_cast<decltype(t.h)>(reinterpret_cast<uint8_t *>(base) +
-                                        (size_t)4 * (q / 2) * n * 32);
-  return t;
-}
-
-template <int Q, typename W, typename H>
-__device__ __forceinline__ void ld_pack(const PackTable<W, H> &t, int idx,
+template <int Q>
+__device__ __forceinline__ void ld_pack(const uint32_t *t, int idx,
                                         uint32_t (&k)[kPackWords<Q>]) {
-  constexpr int NP = Q / 2;
-  if constexpr (NP == 1) {
-    k[0] = t.w[idx];
-  } else if constexpr (NP == 2) {
-    const uint2 v = reinterpret_cast<const uint2 *>(t.w)[idx];
+  if constexpr (kPackWords<Q> == 1) {
+    k[0] = t[idx];
+  } else {
+    const uint2 v = reinterpret_cast<const uint2 *>(t)[idx];
     k[0] = v.x;
     k[1] = v.y;
   }
-  if constexpr ((Q & 1) != 0) k[NP] = t.h[idx];
 }
 
 template <int Q>
-__device__ __forceinline__ void st_pack(const CountTable &t, int idx,
+__device__ __forceinline__ void st_pack(uint32_t *t, int idx,
                                         const uint32_t (&k)[kPackWords<Q>]) {
-  constexpr int NP = Q / 2;
-  if constexpr (NP == 1) {
-    t.w[idx] = k[0];
-  } else if constexpr (NP == 2) {
-    reinterpret_cast<uint2 *>(t.w)[idx] = make_uint2(k[0], k[1]);
+  if constexpr (kPackWords<Q> == 1) {
+    t[idx] = k[0];
+  } else {
+    reinterpret_cast<uint2 *>(t)[idx] = make_uint2(k[0], k[1]);
   }
-  if constexpr ((Q & 1) != 0) t.h[idx] = (uint16_t)k[NP];
 }
 
 // Biased floats 2^23 + d and 2^23 + m of cell slot q (its word w = the
@@ -820,10 +797,10 @@ __device__ __forceinline__ float ex2_approx(float t) {
 struct SumCtx {
   uint16_t *ord;        // [n]: node | parent << 8, in canonical order
   int *hist;            // [32 * ceil(n / 32)]: depth histogram, scratch
-  CountTable cnt;       // [n][32]: every node's packed counts of the
-                        // lane's cells (cnt.w null: none)
-  IncTable inc;         // [n][32]: per-gene packed increments of the
-                        // warp's cells (inc.w null: none)
+  uint32_t *cnt;        // [n][32][NW]: every node's packed counts of the
+                        // lane's cells, or null
+  const uint32_t *inc;  // [n][32][NW]: per-gene packed increments of the
+                        // warp's cells, or null
   const uint8_t *par;   // parent vector of the evaluated tree, or null
 };
 
@@ -1349,7 +1326,7 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
   if (resident) {
     bool inherit = false;
     if constexpr (W32 <= 4)
-      inherit = sx.cnt.w != nullptr && sx.inc.w != nullptr && sx.par != nullptr;
+      inherit = sx.cnt != nullptr && sx.inc != nullptr && sx.par != nullptr;
     if (inherit) {
       if constexpr (W32 <= 4)
         sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
@@ -1502,7 +1479,7 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
   int k = 0, m = 0, bj[Q];
   bool inherit = false;
   if constexpr (W32 <= 4)
-    inherit = resident && sx.cnt.w != nullptr && sx.inc.w != nullptr &&
+    inherit = resident && sx.cnt != nullptr && sx.inc != nullptr &&
               sx.par != nullptr;
   if (inherit) {
     if constexpr (W32 <= 4) {

@@ -40,40 +40,6 @@ __device__ __forceinline__ void copy_rows(const uint32_t *src, uint32_t *dst,
   copy_rows_part<W32>(src, dst, n, 1, 0, lane);
 }
 
-// Shared memory of the chain kernels, in bytes (16-byte aligned pieces).
-__host__ __device__ inline int align16(int b) { return (b + 15) & ~15; }
-
-// Per warp of a chain with the node-order scratch (every sum-score chain:
-// its order is canonical; every chain that inherits counts): the canonical
-// node order, its depth histogram and, with `counts`, the packed counts of
-// every node for the lane's cells (2 q bytes per node and lane).
-__host__ __device__ inline int sum_warp_bytes(int n, int w32, int q,
-                                              bool counts) {
-  return align16(2 * n) + align16(4 * 32 * ((n + 31) / 32)) +
-         (counts && w32 <= 4 ? align16(2 * q * n * 32) : 0);
-}
-
-// One chain slot: two row buffers, the partial sums of both step parities
-// (2 x wpc x 12 words) and a flag word; with the scratch, the current and
-// proposed parent vectors and each warp's scratch.
-__host__ __device__ inline int slot_bytes(int n, int rs, int wpc, bool scratch,
-                                          int w32, int q, bool counts) {
-  int b = 4 * (2 * n * rs + 24 * wpc + 4);
-  if (scratch) b += align16(2 * n) + wpc * sum_warp_bytes(n, w32, q, counts);
-  return b;
-}
-
-// After the slots, with `counts`: the block's tables of per-gene
-// increments, one per warp part of a chain (wpc), each for that warp's
-// 32 q cell slots.
-__host__ __device__ inline int inc_table_bytes(int n, int q) {
-  return align16(2 * q * n * 32);
-}
-__host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
-                                           bool counts) {
-  return counts && w32 <= 4 ? wpc * inc_table_bytes(n, q) : 0;
-}
-
 // The scratch pieces of a slot: parent vectors and warp wic's scratch.
 // (Host-callable too: the layout test walks it over every shape.)
 struct SlotSum {
@@ -94,7 +60,7 @@ __host__ __device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n,
   p += align16(2 * n);
   o.sx.hist = reinterpret_cast<int *>(p);
   p += align16(4 * 32 * ((n + 31) / 32));
-  if (counts && w32 <= 4) o.sx.cnt = pack_table<CountTable>(p, n, q);
+  if (counts && w32 <= 4) o.sx.cnt = reinterpret_cast<uint32_t *>(p);
   return o;
 }
 
@@ -127,9 +93,8 @@ __device__ __forceinline__ void build_increments(uint8_t *table, int wpc,
       }
       k[q >> 1] |= v << (16 * (q & 1));
     }
-    const CountTable t =
-        pack_table<CountTable>(table + (size_t)wic * inc_table_bytes(n, Q), n, Q);
-    st_pack<Q>(t, j * 32 + l, k);
+    st_pack<Q>(reinterpret_cast<uint32_t *>(table + (size_t)wic * inc_table_bytes(n, Q)),
+               j * 32 + l, k);
   }
 }
 
@@ -219,7 +184,7 @@ __device__ __forceinline__ void run_chain(
   uint8_t *cpar = nullptr, *ppar = nullptr;
   bool cur_par_ok = false;  // cpar describes cur
   if constexpr (W32 <= 4) {
-    if (ss.sx.inc.w != nullptr && resident) {
+    if (ss.sx.inc != nullptr && resident) {
       cpar = ss.par0;
       ppar = ss.par1;
       if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
@@ -478,11 +443,11 @@ __device__ __forceinline__ void run_chain(
   if (multi) __syncthreads(); else __syncwarp();
 }
 
-// Resident 128-thread blocks per SM the register budget aims for: fewer
-// cells per lane leave room for more warps.
-template <int W32, int Q>
-struct McmcOccupancy {
-  static constexpr int min_blocks = Q == 1 ? 4 : (Q == 2 ? 3 : 2);
+// Launch bounds of each cells-per-lane variant (bbs_layout.h).
+template <int Q>
+struct ChainBounds {
+  static constexpr int threads = chain_max_threads(Q);
+  static constexpr int min_blocks = chain_min_blocks(Q);
 };
 
 // One dataset: chains 0..n_chains-1, one warp per chain (blocks of `cpb`
@@ -490,7 +455,8 @@ struct McmcOccupancy {
 // moves and/or a step trace (replays and tests); without them the move and
 // trace paths compile away.
 template <int W32, int Q, bool SUM, bool REC>
-__global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
+__global__ void __launch_bounds__(ChainBounds<Q>::threads,
+                                  ChainBounds<Q>::min_blocks)
     mcmc_kernel(const RunArgs a) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int RS = rs_of_w32(W32);
@@ -521,8 +487,8 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
         uint8_t *table = reinterpret_cast<uint8_t *>(smem) + (size_t)cpb * sb;
         build_increments<Q>(table, wpc, a.ds, RS);
         __syncthreads();
-        ss.sx.inc = pack_table<IncTable>(
-            table + (size_t)wic * inc_table_bytes(n, Q), n, Q);
+        ss.sx.inc = reinterpret_cast<const uint32_t *>(
+            table + (size_t)wic * inc_table_bytes(n, Q));
       }
     }
   }
@@ -566,7 +532,7 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
   const uint32_t local = chain - d * (uint32_t)b.chains_per_dataset;
   // the increment table holds the cells of dataset b.table_ds only
   SlotSum ss = ss_in;
-  if ((int)d != b.table_ds) ss.sx.inc = IncTable{nullptr, nullptr};
+  if ((int)d != b.table_ds) ss.sx.inc = nullptr;
   run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
                          nullptr, nullptr, 1, b.states + chain, nullptr,
                          nullptr, b.n_steps, b.cancel, b.status, buf0, buf1,
@@ -576,7 +542,8 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
 // Many datasets: warps take chains from a shared work list (costliest
 // first); each chain brings its own dataset and rules.  One warp per chain.
 template <int W32, int Q, bool SUM>
-__global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
+__global__ void __launch_bounds__(ChainBounds<Q>::threads,
+                                  ChainBounds<Q>::min_blocks)
     batch_kernel(const BatchArgs b) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int RS = rs_of_w32(W32);
@@ -600,7 +567,7 @@ __global__ void __launch_bounds__(128, McmcOccupancy<W32, Q>::min_blocks)
                          (size_t)(blockDim.x >> 5) * sb;
         build_increments<Q>(table, 1, b.ds[b.table_ds], RS);
         __syncthreads();
-        ss.sx.inc = pack_table<IncTable>(table, b.ds[b.table_ds].n_nodes, Q);
+        ss.sx.inc = reinterpret_cast<const uint32_t *>(table);
       }
     }
   }

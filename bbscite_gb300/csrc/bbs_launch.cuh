@@ -23,7 +23,7 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   if (a.wpc > 1) cpb = 1;
   const int threads = 32 * a.wpc * cpb;
-  if (threads > 128) return (int)cudaErrorInvalidConfiguration;
+  if (threads > chain_max_threads(Q)) return (int)cudaErrorInvalidConfiguration;
   const bool counts = inherits_counts(W32, a.ds.n_cells, 32 * a.wpc * Q);
   const size_t smem =
       (size_t)cpb * slot_bytes(a.ds.n_nodes, RS, a.wpc, SUM || counts, W32, Q,
@@ -48,6 +48,7 @@ template <int W32, int Q, bool SUM>
 int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   const int threads = 32 * wpb;
+  if (threads > chain_max_threads(Q)) return (int)cudaErrorInvalidConfiguration;
   const bool counts = b.with_counts != 0;
   if (counts && (W32 > 4 || b.table_ds < 0))
     return (int)cudaErrorInvalidValue;  // counts need one dataset's rows

@@ -206,7 +206,8 @@ BBS_API int bbs_cancel(bbs_ctx *ctx);
  * FPGA pipeline has a fixed chain-group size, src/main.cpp:28-32):
  * cells per lane per chunk (1-4; 1-2 above 128 nodes), warps per chain
  * (1-4; the cells are split over them) and chains per block (one-warp
- * chains only).  0 keeps a value.  bbs_init_chains picks a default. */
+ * chains only: 1-4, or 1-8 with 3-4 cells per lane; a run with a larger
+ * block fails).  0 keeps a value.  bbs_init_chains picks a default. */
 BBS_API int bbs_set_launch(bbs_ctx *ctx, int cells_per_lane,
                            int warps_per_chain, int chains_per_block);
 BBS_API int bbs_get_launch(const bbs_ctx *ctx, int *cells_per_lane,
@@ -315,7 +316,8 @@ BBS_API int bbs_batch_init_chains(bbs_batch *batch, uint32_t chains_per_dataset)
 BBS_API int bbs_batch_run(bbs_batch *batch, uint32_t n_steps);
 BBS_API int bbs_batch_last_run_ms(const bbs_batch *batch, float *ms);
 /* Launch shape: cells per lane (1-4; 1-2 above 128 nodes) and warps per
- * block (1-4);
+ * block (1-4, or 1-8 with 3-4 cells per lane; a run with a larger block
+ * fails);
  * merge_rows != 0 runs 1- and 3-word trees with their 2- and 4-word row
  * stride group (one launch per group instead of two). */
 BBS_API int bbs_batch_set_launch(bbs_batch *batch, int cells_per_lane,

@@ -1,14 +1,13 @@
 // Shared-memory layout of the chain kernels, walked on the host over every
 // shape the launchers accept: node counts 2..256, 1..4 cells per lane,
-// 1..4 warps per chain (one-warp chains 1..4 per block), both scores.  For
+// 1..4 warps per chain (one-warp chains 1..8 per block), both scores.  For
 // each chain slot the pieces the kernels address -- the two row buffers,
 // both parities of the per-warp partial sums, the flag word, the parent
-// vectors, and each warp's node order, depth histogram and count table
-// (its full words and, for an odd number of cells per lane, its 16-bit
-// fields) -- must lie inside the slot, be disjoint and be aligned for their
-// element type; the block's increment tables (one per warp of a chain,
-// split the same way) must lie after the slots and inside the launch's
-// dynamic shared memory.  Prints "layout ok <cases>" or the first
+// vectors, and each warp's node order, depth histogram and count table --
+// must lie inside the slot, be disjoint and be aligned for their element
+// type; the block's increment tables (one per warp of a chain) must lie
+// after the slots and inside the launch's dynamic shared memory, and the
+// launch's size must be the one the host asks for (chain_launch_smem).  Prints "layout ok <cases>" or the first
 // violation (exit status 1).
 #include <cstdint>
 #include <cstdio>
@@ -33,14 +32,12 @@ bool fail(const char *what, int n, int q, int wpc, int cpb, bool sum,
   return false;
 }
 
-// A packed table of n nodes x 32 lanes for q cells per lane: q/2 words per
-// entry (one 32- or 64-bit access) at w, the odd cell's 16-bit fields at h.
-void add_table(std::vector<Piece> &all, const char *name, size_t w, size_t h,
-               int n, int q) {
-  const int np = q / 2;
-  if (np > 0)
-    all.push_back({name, w, w + (size_t)4 * np * n * 32, (size_t)4 * np});
-  if (q & 1) all.push_back({name, h, h + (size_t)2 * n * 32, 2});
+// A packed table of n nodes x 32 lanes for q cells per lane at byte
+// offset w: (q + 1) / 2 words per entry, read as one 32- or 64-bit access.
+void add_table(std::vector<Piece> &all, const char *name, size_t w, int n,
+               int q) {
+  all.push_back({name, w, w + (size_t)bbs::pack_table_bytes(n, q),
+                 (size_t)4 * ((q + 1) / 2)});
 }
 
 // One launch: cpb slots of wpc warps, the tables after them.  `counts`
@@ -55,6 +52,9 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
   const int sb = bbs::slot_bytes(n, rs, wpc, scratch, w32, q, counts);
   const size_t tb = (size_t)bbs::table_bytes(n, w32, q, wpc, counts);
   const size_t total = (size_t)cpb * sb + tb;
+  if (w32 <= 4 && (size_t)bbs::chain_launch_smem(n, counts ? 32 * wpc * q : 32 * wpc * q + 1, q, wpc, cpb, sum) != total)
+    return fail("launch size differs from chain_launch_smem", n, q, wpc, cpb,
+                sum, "");
   std::vector<uint8_t> smem(total + 16);
   uint8_t *base = smem.data();
   std::vector<Piece> all;
@@ -93,10 +93,10 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
           return fail("histogram smaller than n ints", n, q, wpc, cpb, sum, "");
         all.push_back({"hist", off(ss.sx.hist), off(ss.sx.hist) + hist, 4});
         if (counts) {
-          if (ss.sx.cnt.w == nullptr)
+          if (ss.sx.cnt == nullptr)
             return fail("no count table", n, q, wpc, cpb, sum, "");
-          add_table(all, "cnt", off(ss.sx.cnt.w), off(ss.sx.cnt.h), n, q);
-        } else if (ss.sx.cnt.w != nullptr) {
+          add_table(all, "cnt", off(ss.sx.cnt), n, q);
+        } else if (ss.sx.cnt != nullptr) {
           return fail("count table without inherited counts", n, q, wpc,
                       cpb, sum, "");
         }
@@ -110,14 +110,9 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
     const size_t lo = (size_t)cpb * sb;
     if (tb != (size_t)wpc * bbs::inc_table_bytes(n, q))
       return fail("increment tables sized wrongly", n, q, wpc, cpb, sum, "");
-    for (int wic = 0; wic < wpc; wic++) {
-      uint8_t *t = base + lo + (size_t)wic * bbs::inc_table_bytes(n, q);
-      const bbs::IncTable it = bbs::pack_table<bbs::IncTable>(t, n, q);
-      add_table(all, "inc",
-                (size_t)(reinterpret_cast<const uint8_t *>(it.w) - base),
-                (size_t)(reinterpret_cast<const uint8_t *>(it.h) - base), n,
+    for (int wic = 0; wic < wpc; wic++)
+      add_table(all, "inc", lo + (size_t)wic * bbs::inc_table_bytes(n, q), n,
                 q);
-    }
   }
   for (size_t i = 0; i < all.size(); i++) {
     if (all[i].hi > total)
@@ -141,14 +136,14 @@ int main() {
     for (int q = 1; q <= bbs::kMaxQ; q++)
       for (int sum = 0; sum < 2; sum++)
         for (int counts = 0; counts < 2; counts++) {
-          // plain kernel: one-warp chains 1..4 per block, or one chain of
+          // plain kernel: one-warp chains 1..8 per block, or one chain of
           // 2..4 warps
-          for (int cpb = 1; cpb <= 4; cpb++)
+          for (int cpb = 1; 32 * cpb <= bbs::kMaxBlockThreads; cpb++)
             if (!check(n, q, 1, cpb, sum != 0, counts != 0)) return 1;
           for (int wpc = 2; wpc <= 4; wpc++)
             if (!check(n, q, wpc, 1, sum != 0, counts != 0)) return 1;
         }
-  // (the batched kernel's launches are one-warp slots, 1..4 per block: the
+  // (the batched kernel's launches are one-warp slots, 1..8 per block: the
   // cases of the plain kernel with wpc = 1)
   std::printf("layout ok %ld\n", g_cases);
   return 0;

@@ -153,7 +153,7 @@ def test_shared_memory_layout_of_every_launch_shape(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
     assert r.stdout.startswith("layout ok "), r.stdout
-    assert int(r.stdout.split()[2]) == 255 * 4 * 2 * 2 * 7
+    assert int(r.stdout.split()[2]) == 255 * 4 * 2 * 2 * 11
 
 
 def _ctype_of(decl: str):
