@@ -279,13 +279,13 @@ __device__ __forceinline__ void run_chain(
     if (multi) __syncthreads(); else __syncwarp();
     // The evaluated tree's parent vector.  It is checked against the rows
     // where it can be wrong -- a proposal whose move took node 0 by
-    // fallback -- and, conservatively, on every tree of a multi-warp chain,
-    // and used only where it checks out; checked builds check every one and
-    // record a mismatch outside those cases as a failed device check.
+    // fallback -- and used only where it checks out; checked builds check
+    // every one and record a mismatch outside that case as a failed device
+    // check.
     bool par_ok = false;
     if constexpr (W32 <= 4) {
       if (cpar != nullptr && cur_par_ok) {
-        const bool suspect = multi || (scored != cur && fallback_move);
+        const bool suspect = scored != cur && fallback_move;
         bool check = suspect;
 #ifdef BBS_CHECKED
         check = true;
