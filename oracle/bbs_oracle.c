@@ -951,6 +951,20 @@ static void *orc_proxy_worker(void *arg) {
   return NULL;
 }
 
+/* The scores of n_trees trees (dmq: n_trees x 2 x 128 words), one by one:
+ * the per-tree values the benchmark loop sums. */
+void orc_cpu_proxy_scores(float alpha, float beta, const uint64_t *mutq,
+                          const uint64_t *knownq, const uint64_t *dmq,
+                          uint32_t n_trees, float *out) {
+  float L[2][2];
+  L[0][0] = (float)log(1.0 - (double)alpha);
+  L[1][0] = logf(alpha);
+  L[0][1] = logf(beta);
+  L[1][1] = (float)log(1.0 - (double)beta);
+  for (uint32_t t = 0; t < n_trees; t++)
+    out[t] = orc_proxy_score(L, mutq, knownq, dmq + t * 256);
+}
+
 double orc_cpu_scoring_proxy(float alpha, float beta, const uint64_t *mutq,
                              const uint64_t *knownq, const uint64_t *dmq,
                              uint32_t n_trees, uint32_t reps,

@@ -211,6 +211,9 @@ float orc_run_chains_mt(const orc_chain_params *cp,
  * bits.  Runs `n_trees` x `reps` scorings over n_threads threads and
  * returns the checksum of scores.
  */
+void orc_cpu_proxy_scores(float alpha, float beta, const uint64_t *mutq,
+                          const uint64_t *knownq, const uint64_t *dmq,
+                          uint32_t n_trees, float *out);
 double orc_cpu_scoring_proxy(float alpha, float beta, const uint64_t *mutq,
                              const uint64_t *knownq, const uint64_t *dmq,
                              uint32_t n_trees, uint32_t reps,

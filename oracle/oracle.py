@@ -371,6 +371,25 @@ def run_chains_mt(alpha, beta_mean, beta_sd, gamma, mp, seed, parents, mut,
     return float(best), finals
 
 
+def cpu_proxy_scores(alpha, beta, mutq, knownq, dmq, reference=False):
+    """Per-tree scores of the CPUTreeScorer proxy at 128 cells x 127 genes
+    (mutq / knownq: [quadword][cell] words, dmq: trees x [quadword][node]),
+    by the restatement or, with reference=True, by the reference's own
+    class (None when oracle/_ref was not built)."""
+    n = dmq.shape[0]
+    out = np.zeros(n, dtype=np.float32)
+    args = (C.c_float(alpha), C.c_float(beta), _p(mutq), _p(knownq), _p(dmq),
+            C.c_uint32(n), _p(out))
+    if reference:
+        r = ref_lib()
+        if r is None:
+            return None
+        r.ref_proxy_scores(*args)
+    else:
+        lib().orc_cpu_proxy_scores(*args)
+    return out
+
+
 def cpu_scoring_proxy(alpha, beta, mutq, knownq, dmq, n_trees, reps,
                       n_threads) -> float:
     return float(lib().orc_cpu_scoring_proxy(alpha, beta, _p(mutq),

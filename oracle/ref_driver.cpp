@@ -5,8 +5,8 @@
 //
 // TEST INFRASTRUCTURE ONLY.  Built by oracle/Makefile into
 // oracle/_ref/libbbs_ref.so when the reference sources are present; used
-// by tests/golden/make_golden.py and tests/test_oracle_vs_ref.py to pin
-// the C restatement in oracle/bbs_oracle.c.  The chain loop below restates
+// by tests/golden/make_golden.py and tests/test_oracle.py to pin the C
+// restatement in oracle/bbs_oracle.c.  The chain loop below restates
 // src/Application.hpp:408-487 (the only part of Application.hpp that needs
 // the FPGA runtime) around the reference's classes.
 #include <MutationTree.hpp>

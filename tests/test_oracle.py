@@ -444,3 +444,40 @@ def test_application_kat_on_the_oracle(orc, kat):
     r, _, _, _ = orc.logscore_tree(k["alpha"], k["beta"], k["beta_sd"], dm,
                                    mut, known, k["beta"])
     assert best == pytest.approx(float(r), rel=1e-5)
+
+
+def test_cpu_proxy_restatement_matches_reference_class(orc):
+    """orc_cpu_proxy_scores -- the restated CPUTreeScorer that the CPU
+    baseline times -- gives the reference class's scores bit for bit
+    (tests/golden/proxy_vectors.npz, made from
+    cpu_scoring_benchmark/CPUTreeScorer.hpp compiled unmodified)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)),
+                             "golden", "proxy_vectors.npz"))
+    for i in range(3):
+        a, b = (float(x) for x in g[f"rates{i}"])
+        s = orc.cpu_proxy_scores(a, b, g["mutq"], g["knownq"], g["dmq"])
+        assert s.view(np.uint32).tolist() == \
+            g[f"scores{i}"].view(np.uint32).tolist()
+
+
+def test_cpu_proxy_vectors_regenerate(orc, tmp_path):
+    """tests/golden/proxy_vectors.npz is what its generator makes from the
+    reference's own class (needs oracle/_ref, built only where the
+    reference sources are)."""
+    import importlib.util
+    import os
+    if orc.ref_lib() is None:
+        pytest.skip("oracle/_ref is not built here")
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    spec = importlib.util.spec_from_file_location(
+        "make_proxy_golden", os.path.join(here, "make_proxy_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    mg.OUT = str(tmp_path / "proxy_vectors.npz")
+    mg.main()
+    old = np.load(os.path.join(here, "proxy_vectors.npz"))
+    new = np.load(mg.OUT)
+    assert sorted(old.files) == sorted(new.files)
+    for k in old.files:
+        assert old[k].tobytes() == new[k].tobytes(), k
