@@ -360,10 +360,16 @@ BBS_API int bbs_sumscore_grad(bbs_ctx *ctx, const uint64_t *dm, const float *alp
  * lives in a fixed device array of BBS_NOALLOC_MAX_TREES entries (256 KB),
  * which every GPU that loads this library holds until the process exits;
  * more trees per call are rejected with BBS_ERR_SIZE.  The first call on a
- * device looks that array's address up (cudaGetSymbolAddress); make it
- * before any stream capture.  All calls share the array, so calls that
- * overlap on the GPU (several host threads or contexts at once) race;
- * serialise them.  The context's device must be the current device. */
+ * device looks that array's address up (cudaGetSymbolAddress) and keeps it
+ * for the life of the process; make that first call before any stream
+ * capture.  The kept address does not survive cudaDeviceReset: do not call
+ * this entry point again after resetting the device.  All calls share the
+ * array, so calls that overlap on the GPU (several host threads or
+ * contexts at once) race; serialise them.  The context's device must be
+ * the current device.  The call runs on the context's own stream, not the
+ * caller's, and returns when the scores are written (it waits for that
+ * stream): finish writing dm_device (synchronise the stream that produced
+ * it) before the call. */
 #define BBS_NOALLOC_MAX_TREES 16384
 BBS_API int bbs_score_trees_noalloc(bbs_ctx *ctx, const uint64_t *dm_device,
                                     const float *betas, uint32_t n_trees,

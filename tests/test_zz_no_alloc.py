@@ -66,6 +66,39 @@ def test_noalloc_matches_score_trees_twice(native):
             np.testing.assert_array_equal(got_c, want_c)
 
 
+@pytest.mark.parametrize("G,Cn,with_counts", [(255, 40, True),
+                                               (95, 96, False)])
+def test_noalloc_wide_rows_and_no_counts(native, G, Cn, with_counts):
+    """Rows of four 64-bit words (255 genes), and a call without the
+    optional counts buffer: the same scores as bbs_score_trees."""
+    torch = pytest.importorskip("torch")
+    fn = _bind(native)
+    m, _, _ = D.generate_dataset(G + Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    p = native.default_params(alpha_mean=1e-3, beta_mean=0.2)
+    rng = np.random.default_rng(G)
+    with native.Context(mut, known, Cn, G, p) as ctx:
+        for n_trees in (70, 5):
+            dm = _random_trees(native, rng, G, n_trees)
+            betas = rng.uniform(0.05, 0.6, size=n_trees).astype(np.float32)
+            want_s, want_c, _ = ctx.score_trees(dm, betas)
+            d_dm = torch.from_numpy(dm.view(np.int64).copy()).cuda()
+            d_scores = torch.full((n_trees,), float("nan"),
+                                  dtype=torch.float32, device="cuda")
+            d_counts = (torch.zeros((n_trees, 4), dtype=torch.int64,
+                                    device="cuda") if with_counts else None)
+            torch.cuda.synchronize()
+            rc = fn(ctx._h, C.c_void_p(d_dm.data_ptr()),
+                    betas.ctypes.data_as(C.c_void_p), n_trees,
+                    C.c_void_p(d_scores.data_ptr()),
+                    C.c_void_p(d_counts.data_ptr()) if with_counts else None)
+            native.check(rc)
+            np.testing.assert_array_equal(d_scores.cpu().numpy(), want_s)
+            if with_counts:
+                np.testing.assert_array_equal(
+                    d_counts.cpu().numpy().view(np.uint64), want_c)
+
+
 def test_noalloc_rejects_too_many_trees(native):
     torch = pytest.importorskip("torch")
     fn = _bind(native)
