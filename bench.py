@@ -83,7 +83,12 @@ def parse_args(argv=None):
                     help="batched form: cells_per_lane,warps_per_block,"
                          "merge_rows")
     ap.add_argument("--mix-datasets", type=int, default=512)
-    ap.add_argument("--mix-steps", type=int, default=1000)
+    ap.add_argument("--mix-steps", type=int, default=20000,
+                    help="512-dataset mix: steps per chain of the batched "
+                         "and the sequential plain form")
+    ap.add_argument("--mix-tuned-steps", type=int, default=2000,
+                    help="512-dataset mix: steps per chain of the tuned "
+                         "single-dataset form")
     ap.add_argument("--lvr-steps", type=int, default=400000,
                     help="Langevin vs random walk: steps per chain (0: off)")
     ap.add_argument("--lvr-seeds", type=int, default=4)
@@ -205,7 +210,7 @@ def cpu_baseline(seconds: float, rank: int = 0) -> dict:
                               score_mode=0)
     dt = time.perf_counter() - t0
     return {"value": n_chains * steps / dt, "unit": UNIT, "cores": threads,
-            "kind": "port",
+            "kind": "port", "chains": n_chains,
             "sample": f"{n_chains} chains x {steps} steps of the 95x96 "
                       f"workload ({dt:.1f} s), oracle/bbs_oracle.c "
                       "orc_run_chains_mt, reference cell-order score",
@@ -258,6 +263,15 @@ def cpu_scoring_proxy_rate(seconds: float) -> dict:
                       "orc_cpu_scoring_proxy"}
 
 
+# What ties the CPU port to the reference's own code: the box has no
+# reference sources, so the reference's classes cannot be compiled there.
+PORT_PINNING = ("oracle/bbs_oracle.c restates the reference's step loop "
+                "(src/Application.hpp:408-487) and scorer; it reproduces the "
+                "reference classes compiled unmodified bit for bit (golden "
+                "chains, scores and moves in tests/golden/ref_vectors.npz, "
+                "CPUTreeScorer scores in tests/golden/proxy_vectors.npz)")
+
+
 def run_reference(args) -> None:
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -278,15 +292,18 @@ def run_reference(args) -> None:
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64-popcount+f32", "data": "synthetic",
         "config": {"workload": f"{w['n_genes']} genes x {w['n_cells']} "
-                   f"cells, {args.chains} chains; data alpha=1e-3 beta=0.2 "
-                   "(10% unknown, 2% homozygous); the reference's plain "
-                   "MCMC at fixed error rates (it has no batched or adjoint "
-                   "form)",
+                   f"cells; a bounded sample of {info['chains']} chains of "
+                   f"the {args.chains}-chain workload is timed; data "
+                   "alpha=1e-3 beta=0.2 (10% unknown, 2% homozygous); the "
+                   "reference's plain MCMC at fixed error rates (it has no "
+                   "batched or adjoint form)",
                    "n_genes": w["n_genes"], "n_cells": w["n_cells"],
-                   "chains": args.chains,
+                   "chains": info["chains"],
+                   "workload_chains": args.chains,
                    "parallelism": "host threads over chains"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"],
-                         "kind": info["kind"], "sample": info["sample"]},
+                         "kind": info["kind"], "sample": info["sample"],
+                         "pinned": PORT_PINNING},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "best_logl": info["best_logl"],
@@ -296,17 +313,20 @@ def run_reference(args) -> None:
 
 # ------------------------------------------------------------------ ours --
 
-def _traffic_from_profile(name="batch_95x96_dram.json",
-                          key="dram_bytes_per_chain_per_launch"):
-    """A figure of a chain kernel from the committed ncu summary under
-    profiles/ (DRAM bytes per chain per launch, or warp instructions per
-    chain-step), or None."""
-    p = os.path.join(ROOT, "profiles", name)
+PROFILE = "chain_kernels_95x96.json"
+
+
+def _profile_figure(form: str, key: str):
+    """A figure of a chain kernel at the bench's shape from the committed
+    ncu summary profiles/chain_kernels_95x96.json (form "batch" or
+    "plain"; warp instructions per chain-step, DRAM bytes per chain per
+    launch), or None."""
+    p = os.path.join(ROOT, "profiles", PROFILE)
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
-    return d.get(key)
+    return d.get(form, {}).get(key)
 
 
 def max_over_ranks(dist, values, device):
@@ -377,12 +397,15 @@ def mix_datasets(n_datasets: int, seed: int = 512):
     return out
 
 
-def run_mix(N, n_datasets, chains, steps, flush, torch):
+def run_mix(N, n_datasets, chains, steps, flush, torch, tuned_steps=None):
     """Batched launch (autotuned, CUDA graph) vs one plain launch per
-    dataset, device time of the runs only.  The plain form runs each chain
-    on one warp (cells_per_lane = min(ceil(C/32), 4), one chain per block);
-    the tuned single-dataset form lets each launch spread a chain's cells
-    over up to 4 warps (the context's default launch heuristic)."""
+    dataset, device time of the runs only, `steps` steps per chain in both.
+    The plain form runs each chain on one warp (cells_per_lane =
+    min(ceil(C/32), 4), one chain per block); the tuned single-dataset form
+    (timed over tuned_steps steps per chain) lets each launch spread a
+    chain's cells over up to 4 warps (the context's default launch
+    heuristic)."""
+    tuned_steps = tuned_steps or steps
     mix = mix_datasets(n_datasets)
     params = [N.default_params(alpha_mean=a, beta_mean=b, seed=900 + i)
               for i, (_, a, b) in enumerate(mix)]
@@ -399,20 +422,23 @@ def run_mix(N, n_datasets, chains, steps, flush, torch):
     for i, ((mut, known, Cn, G), _, _) in enumerate(mix):
         with N.Context(mut, known, Cn, G, params[i]) as c:
             c.init_chains(chains)
-            c.run(steps)
+            c.run(tuned_steps)
             tuned_ms += c.last_run_ms()
             c.init_chains(chains)
             c.set_launch(min((Cn + 31) // 32, 4), 1, 1)
             c.run(steps)
             plain_ms += c.last_run_ms()
     total = n_datasets * chains * steps
+    tuned_rate = n_datasets * chains * tuned_steps / (tuned_ms / 1e3)
+    batched_rate = total / (batched_ms / 1e3)
     return {"datasets": n_datasets, "chains_per_dataset": chains,
             "steps": steps,
-            "batched_chain_steps_per_s": total / (batched_ms / 1e3),
+            "batched_chain_steps_per_s": batched_rate,
             "sequential_plain_chain_steps_per_s": total / (plain_ms / 1e3),
             "speedup": plain_ms / batched_ms,
-            "sequential_tuned_chain_steps_per_s": total / (tuned_ms / 1e3),
-            "speedup_vs_tuned_single": tuned_ms / batched_ms,
+            "tuned_steps": tuned_steps,
+            "sequential_tuned_chain_steps_per_s": tuned_rate,
+            "speedup_vs_tuned_single": batched_rate / tuned_rate,
             "pairs_per_chain_step": mix_pairs(mix),
             "batched_launch": {"cells_per_lane": shape[0],
                                "warps_per_block": shape[1],
@@ -507,12 +533,13 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
         # never reached within the run: null in the JSON line
         return None if math.isinf(med) else med
 
-    per_seed = [{"best": {a: res[a][sd]["best"][-1] for a in arms},
+    per_seed = [{"best": {a: round(res[a][sd]["best"][-1], 3) for a in arms},
                  "steps_to_rw_best": {a: steps_to(a, sd, "random_walk")
                                       for a in arms},
                  "steps_to_reference_best": {
                      a: steps_to(a, sd, "reference_beta_walk") for a in arms},
-                 "best_at_own_rates": {a: res[a][sd]["own"] for a in arms}}
+                 "best_at_own_rates": {a: round(res[a][sd]["own"], 3)
+                                       for a in arms}}
                 for sd in range(seeds)]
     ratios = {a: median_ratio(a, "random_walk") for a in arms
               if a not in ("random_walk", "reference_beta_walk")}
@@ -581,9 +608,11 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
     popc = popc_per_chain_step(G, Cn)
     peak, _ = N.popc_peak()
     out["popc_per_chain_step"] = popc
-    out["batched_adjoint_frac"] = \
+    # POPC-equivalent work (the masked-popcount formulation's count)
+    out["batched_adjoint_popc_equivalent_frac"] = \
         out["batched_adjoint_chain_steps_per_s"] * popc / peak
-    out["plain_frac"] = out["plain_chain_steps_per_s"] * popc / peak
+    out["plain_popc_equivalent_frac"] = \
+        out["plain_chain_steps_per_s"] * popc / peak
     return out
 
 
@@ -683,25 +712,49 @@ def run_ours(args) -> None:
     s_adj = [global_best(dist, s_adj[0], rank, ws, "cuda")[0]]
     s_pl = [global_best(dist, s_pl[0], rank, ws, "cuda")[0]]
 
-    # roofline of the headline kernel (integer pipe: POPC)
+    # roofline of the headline kernel.  The binding resource is the issue
+    # slot: four warp instructions per clock per SM, against the profiled
+    # instructions per chain-step of the benched kernel (ncu).  The POPC
+    # count of the masked-popcount formulation is kept as equivalent work.
+    rate = chains * L / (statistics.mean(adj_list) / 1e3)
+    plain_rate = chains * L / (statistics.mean(pl_list) / 1e3)
     popc_step = popc_per_chain_step(G, Cn)
-    achieved = popc_step * chains * L / (statistics.mean(adj_list) / 1e3)
-    peak, clk_hz = N.popc_peak()
-    traffic = _traffic_from_profile()
-    # the binding resource: issue slots, four warp instructions per clock
-    # per SM, against the profiled instructions per chain-step
-    inst_step = _traffic_from_profile(key="warp_instructions_per_chain_step")
-    issue = None
-    if inst_step is not None:
-        sms = torch.cuda.get_device_properties(0).multi_processor_count
-        rate = chains * L / (statistics.mean(adj_list) / 1e3)
-        issue_peak = 4.0 * sms * clk_hz
-        issue = {"achieved": rate * inst_step / 1e9, "peak": issue_peak / 1e9,
-                 "unit": "G warp-instructions/s", "frac": rate * inst_step /
-                 issue_peak, "instructions_per_chain_step": inst_step,
-                 "source": "smsp__inst_executed.sum per chain-step, "
-                           "profiles/batch_95x96_dram.json; peak 4 per "
-                           "clock per SM at the measured SM clock"}
+    popc_peak, clk_hz = N.popc_peak()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    issue_peak = 4.0 * sms * clk_hz
+    inst_step = _profile_figure("batch", "warp_instructions_per_chain_step")
+    inst_plain = _profile_figure("plain", "warp_instructions_per_chain_step")
+    dram = _profile_figure("batch", "dram_bytes_per_chain_per_launch")
+
+    def issue_frac(r, inst):
+        return None if inst is None else r * inst / issue_peak
+
+    roofline = {
+        "bound": "issue",
+        "achieved": None if inst_step is None else rate * inst_step / 1e9,
+        "peak": issue_peak / 1e9, "unit": "G warp-instructions/s",
+        "frac": issue_frac(rate, inst_step),
+        "traffic": (dram * chains) if dram is not None else None,
+        "traffic_unit": "DRAM bytes per launch (ncu dram__bytes_read.sum + "
+                        f"dram__bytes_write.sum, profiles/{PROFILE})",
+        "peak_source": f"4 warp instructions per clock per SM x {sms} SMs "
+                       f"at the SM clock measured live ({clk_hz / 1e6:.0f} "
+                       "MHz, bbs_popc_peak)",
+        "work_per_chain_step": f"{inst_step} warp instructions "
+                               "(smsp__inst_executed.sum of the benched "
+                               f"kernel per chain-step, profiles/{PROFILE})",
+        "plain_frac": issue_frac(plain_rate, inst_plain),
+        "plain_work_per_chain_step": inst_plain,
+        "equivalent_work": {
+            "unit": "G POPC/s", "achieved": rate * popc_step / 1e9,
+            "peak": popc_peak / 1e9, "frac": rate * popc_step / popc_peak,
+            "plain_frac": plain_rate * popc_step / popc_peak,
+            "per_chain_step": popc_step,
+            "note": "32-bit POPC of the masked-popcount formulation "
+                    "(cells x nodes x 2 x ceil(genes/32)); the benched "
+                    "kernels inherit counts and issue none of them in the "
+                    "node loop, so this is work done, not a pipe's use"},
+    }
 
     # end to end through the C ABI with host buffers (batched+adjoint)
     e2e_times = []
@@ -723,7 +776,8 @@ def run_ours(args) -> None:
 
     mix = lvr = caps = None
     if rank == 0 and args.mix_datasets > 0:
-        mix = run_mix(N, args.mix_datasets, 32, args.mix_steps, flush, torch)
+        mix = run_mix(N, args.mix_datasets, 32, args.mix_steps, flush, torch,
+                      args.mix_tuned_steps)
     if rank == 0 and args.lvr_steps > 0:
         lvr = run_langevin_vs_rw(N, mut, known, G, Cn, args.lvr_chains,
                                  args.lvr_steps, args.lvr_seeds,
@@ -771,23 +825,7 @@ def run_ours(args) -> None:
             "within_0.1_nats": bool(s_adj[0] >= s_pl[0] - 0.1),
             "learned_alpha": ab["alpha"], "learned_beta": ab["beta"],
         },
-        "roofline": {
-            "bound": "int (POPC-equivalent work; issue slots bind, see issue)",
-            "achieved": achieved / 1e9,
-            "peak": peak / 1e9, "unit": "Gop/s",
-            "frac": achieved / peak,
-            "traffic": (traffic * chains) if traffic is not None else None,
-            "traffic_unit": "bytes per launch (ncu dram read+write, "
-                            "profiles/batch_95x96_dram.json)",
-            "peak_source": "bbs_popc_peak microbenchmark on this GPU "
-                           f"(SM clock {clk_hz / 1e6:.0f} MHz)",
-            "work_per_chain_step": f"{popc_step} POPC (32-bit) of the "
-                                   "masked-popcount formulation; the sum "
-                                   "score inherits counts and issues none",
-            "plain_frac": popc_step * chains * L /
-            (statistics.mean(pl_list) / 1e3) / peak,
-            "issue": issue,
-        },
+        "roofline": roofline,
         "counted_tbit_per_s": value * counted_bits_per_chain_step(G, Cn)
         / 1e12,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -795,18 +833,43 @@ def run_ours(args) -> None:
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
-    if mix is not None:
-        out["batched_mix"] = mix
     if lvr is not None:
         out["langevin_vs_random_walk"] = lvr
     if caps is not None:
         out["beyond_caps_255x512"] = caps
+    if mix is not None:
+        out["batched_mix"] = mix
+    cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         b = cpu_baseline(args.cpu_seconds)
+        cpu = b["value"]
         out["cpu_baseline"] = {k: b[k] for k in
                                ("value", "unit", "cores", "kind", "sample")}
+        out["cpu_baseline"]["pinned"] = PORT_PINNING
         out["cpu_baseline"]["scoring_proxy"] = cpu_scoring_proxy_rate(
             min(5.0, args.cpu_seconds))
+        # like for like: the plain form runs the reference's max score at
+        # fixed rates, as the CPU port does; the headline form also learns
+        # the rates with the sum score (a cross-form comparison)
+        out["vs_cpu"] = {
+            "plain_over_cpu": plain_value / cpu,
+            "plain_e2e_basis": "device time",
+            "batched_adjoint_over_cpu_cross_form": value / cpu,
+            "batched_adjoint_e2e_over_cpu_cross_form": e2e_value / cpu,
+        }
+    # the key figures once more, last, where a tail of the line keeps them
+    out["summary"] = {
+        "batched_adjoint": value, "plain": plain_value,
+        "e2e": e2e_value, "issue_frac": roofline["frac"],
+        "plain_issue_frac": roofline["plain_frac"],
+        "plain_over_cpu": plain_value / cpu if cpu else None,
+        "mix_speedup": mix["speedup"] if mix else None,
+        "mix_steps": mix["steps"] if mix else None,
+        "langevin_half_met": lvr["target_half_met"] if lvr else None,
+        "caps_batched_adjoint":
+            caps["batched_adjoint_chain_steps_per_s"] if caps else None,
+        "caps_plain": caps["plain_chain_steps_per_s"] if caps else None,
+    }
     if rank == 0:
         print(json.dumps(out), flush=True)
     if dist is not None:

@@ -26,9 +26,12 @@ def test_reference_arm_prints_one_contract_line():
     assert (d["n_gpus"], d["steps"], d["warmup"]) == (1, 1, 0)
     assert d["value"] > 0
     w = bench.WORKLOAD
+    # the workload of the GPU arm; the chains named are those timed
     assert (d["config"]["n_genes"], d["config"]["n_cells"],
-            d["config"]["chains"]) == (w["n_genes"], w["n_cells"],
-                                       w["chains"])
+            d["config"]["workload_chains"]) == (w["n_genes"], w["n_cells"],
+                                                w["chains"])
+    assert 1 <= d["config"]["chains"] <= w["chains"]
+    assert f"{d['config']['chains']} chains" in d["cpu_baseline"]["sample"]
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1
