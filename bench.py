@@ -91,7 +91,7 @@ def parse_args(argv=None):
                          "single-dataset form")
     ap.add_argument("--lvr-steps", type=int, default=400000,
                     help="Langevin vs random walk: steps per chain (0: off)")
-    ap.add_argument("--lvr-seeds", type=int, default=4)
+    ap.add_argument("--lvr-seeds", type=int, default=8)
     ap.add_argument("--lvr-chains", type=int, default=256)
     ap.add_argument("--lvr-error-step", type=float, default=1.2)
     ap.add_argument("--caps-steps", type=int, default=500,
@@ -462,7 +462,9 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     seeds (the same Philox seeds in every arm).  Arms: the preconditioned
     random walk on (logit alpha, logit beta) with the reference's max
     score; the reference's own beta random walk (alpha stays at its
-    start); Langevin with the sum score; Langevin with the max score.  At
+    start); Langevin with the sum score; Langevin with the max score; and,
+    as the bound no error-rate move can beat, the reference's chain
+    started at the generator's rates (true_rates).  At
     every checkpoint (1,000-step chunks to 20,000 steps, then 10,000-step
     chunks) each arm's best tree is scored with the reference's max score
     at the generator's rates (a scale common to all arms: the chains rank
@@ -474,20 +476,25 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     values."""
     import numpy as np
 
-    arms = {"random_walk": (N.SCORE_MAX, N.ERROR_RANDOM_WALK),
-            "langevin": (N.SCORE_SUM, N.ERROR_LANGEVIN),
-            "langevin_max_score": (N.SCORE_MAX, N.ERROR_LANGEVIN),
+    start = (1e-2, 0.3)
+    arms = {"random_walk": (N.SCORE_MAX, N.ERROR_RANDOM_WALK, start),
+            "langevin": (N.SCORE_SUM, N.ERROR_LANGEVIN, start),
+            "langevin_max_score": (N.SCORE_MAX, N.ERROR_LANGEVIN, start),
             # the reference's own chain: its beta random walk (ChangeBeta,
             # src/MutationTree.hpp:345-351), alpha fixed at its start
-            "reference_beta_walk": (N.SCORE_MAX, N.ERROR_BETA_WALK)}
+            "reference_beta_walk": (N.SCORE_MAX, N.ERROR_BETA_WALK, start),
+            # the bound: the reference's chain started at the generator's
+            # rates, which no error-rate move can learn faster than
+            "true_rates": (N.SCORE_MAX, N.ERROR_BETA_WALK,
+                           (data_alpha, data_beta))}
     marks = list(range(1000, 20001, 1000)) + \
         list(range(30000, total + 1, 10000))
     res = {a: [] for a in arms}
     sp = N.default_params(alpha_mean=data_alpha, beta_mean=data_beta)
     with N.Context(mut, known, Cn, G, sp) as scorer:
         for sd in range(seeds):
-            for name, (mode, move) in arms.items():
-                p = N.default_params(alpha_mean=1e-2, beta_mean=0.3,
+            for name, (mode, move, (a0, b0)) in arms.items():
+                p = N.default_params(alpha_mean=a0, beta_mean=b0,
                                      seed=0x1A6E + 7919 * sd,
                                      prob_beta_change=0.1, score_mode=mode,
                                      error_move=move, error_step=error_step)
@@ -544,15 +551,23 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     ratios = {a: median_ratio(a, "random_walk") for a in arms
               if a not in ("random_walk", "reference_beta_walk")}
     ratios_ref = {a: median_ratio(a, "reference_beta_walk") for a in arms
-                  if a not in ("random_walk", "reference_beta_walk")}
+                  if a not in ("random_walk", "reference_beta_walk",
+                               "true_rates")}
     return {
         "chains": chains, "steps": total, "seeds": seeds,
         "error_step": error_step, "n_genes": G, "n_cells": Cn,
         "scored_with": f"reference max score at alpha={data_alpha:g} "
                        f"beta={data_beta:g}",
         "arms": {a: {"score": "sum" if m == N.SCORE_SUM else "max",
-                     "error_move": "langevin" if e == N.ERROR_LANGEVIN
-                     else "random_walk"} for a, (m, e) in arms.items()},
+                     "error_move": {N.ERROR_LANGEVIN: "langevin",
+                                    N.ERROR_RANDOM_WALK: "random_walk",
+                                    N.ERROR_BETA_WALK: "beta_walk"}[e],
+                     "start": [a0, b0]}
+                 for a, (m, e, (a0, b0)) in arms.items()},
+        # steps-to-best of a chain that knows the rates from step 0: no
+        # error-rate move can do better than this, so a ratio above 0.5
+        # here says the target is set by the shared tree moves
+        "true_rates_step_ratio_over_rw": ratios["true_rates"],
         "per_seed": per_seed,
         "median_step_ratio_over_rw": ratios,
         "median_step_ratio_over_reference_beta_walk": ratios_ref,

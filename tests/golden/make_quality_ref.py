@@ -1,5 +1,5 @@
 """Generates tests/golden/quality_ref.json: the reference's best-found
-log-likelihoods on 32 seeded datasets of the 63-gene x 64-cell workload
+log-likelihoods on 64 seeded datasets of the 63-gene x 64-cell workload
 (alpha=6.04e-5, beta=0.4309, 5% unknown, no homozygous entries), with
 8 chains x 100,000 steps each.
 
@@ -34,7 +34,7 @@ OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)),
                    "quality_ref.json")
 WORKLOAD = dict(n_genes=63, n_cells=64, alpha=6.04e-5, beta=0.4309,
                 beta_sd=0.1, missing=0.05, homozygous=0.0, chains=8,
-                steps=100000, datasets=32, seed0=3100)
+                steps=100000, datasets=64, seed0=3100)
 
 
 def run_dataset(i: int) -> dict:

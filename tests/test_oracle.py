@@ -322,7 +322,7 @@ def test_quality_fixture_scores(orc):
     with open(path) as f:
         fx = json.load(f)
     w = fx["workload"]
-    assert len(fx["results"]) == w["datasets"] == 32
+    assert len(fx["results"]) == w["datasets"] == 64
     for row in fx["results"][:8]:
         m, _, _ = D.generate_dataset(row["dataset_seed"], w["n_genes"],
                                      w["n_cells"], w["alpha"], w["beta"],
