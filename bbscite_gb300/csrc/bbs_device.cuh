@@ -62,18 +62,14 @@ __device__ __forceinline__ float u01_24(uint32_t x) {
   return __uint2float_rn(x >> 8) * 5.9604644775390625e-08f;
 }
 
-// The normal jump is only drawn when it is used (beta moves) or recorded.
-__device__ __forceinline__ bbs_raw_move sample_move(const MoveProbs &mp,
-                                                    uint32_t n_nodes,
-                                                    uint64_t seed,
-                                                    uint32_t chain,
-                                                    uint64_t step,
-                                                    bool always_jump) {
-  const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
-  const uint4 a = philox4x32_10(
-      make_uint4((uint32_t)step, (uint32_t)(step >> 32), chain, 0u), key);
-  const uint4 b = philox4x32_10(
-      make_uint4((uint32_t)step, (uint32_t)(step >> 32), chain, 1u), key);
+// The move of one step from its two Philox blocks a = Philox(step, chain,
+// 0) and b = Philox(step, chain, 1) under the key (seed).  The normal jump
+// is only drawn when it is used (beta moves) or recorded.
+__device__ __forceinline__ bbs_raw_move move_from_words(const MoveProbs &mp,
+                                                        uint32_t n_nodes,
+                                                        const uint4 a,
+                                                        const uint4 b,
+                                                        bool always_jump) {
   bbs_raw_move m;
   const float ut = u01_24(a.x);
   m.move_type = ut <= mp.cum_beta    ? BBS_MOVE_CHANGE_BETA
@@ -99,6 +95,21 @@ __device__ __forceinline__ bbs_raw_move sample_move(const MoveProbs &mp,
   }
   m.reserved = 0;
   return m;
+}
+
+// The Philox blocks of 16 consecutive steps, computed by the whole warp at
+// once: lane l computes block (l & 1) of step step0 + (l >> 1) into
+// buf[l] (a warp's kPhiloxBytes of shared memory).  Step step0 + k then
+// reads its two blocks buf[2k] and buf[2k + 1]: one Philox evaluation per
+// lane for 16 steps instead of two per step.
+__device__ __forceinline__ void philox_fill(uint4 *buf, uint64_t seed,
+                                            uint32_t chain, uint64_t step0,
+                                            int lane) {
+  const uint2 key = make_uint2((uint32_t)seed, (uint32_t)(seed >> 32));
+  const uint64_t step = step0 + (uint64_t)(lane >> 1);
+  buf[lane] = philox4x32_10(make_uint4((uint32_t)step, (uint32_t)(step >> 32),
+                                       chain, (uint32_t)(lane & 1)),
+                            key);
 }
 
 // ------------------------------------------------------------------------
@@ -743,12 +754,24 @@ __device__ __forceinline__ LogTable2 log_table2(const LogTable &L, float nz) {
 // in (d, m) = (popc(D & A), popc(M & A)), two FMAs per pair.  Adds to
 // acc[6], in fixed point (2^-16 units for scores, 2^-20 for counts, so the
 // result does not depend on how cells are split over lanes and warps):
-// sum_c lse_c, the expected class counts E[n00], E[n01], E[n10], E[n11],
-// and sum_c max_j s_cj (the max score).
+// [0] sum_c lse_c, [2] E[n01] and [4] E[n11] (the expected class counts
+// of observed-0 and observed-1 bits under the attachment posterior) and
+// [5] sum_c max_j s_cj (the max score).  [1] and [3], E[n00] and E[n10],
+// are left to the caller: with every cell counted they are the dataset's
+// totals of observed-0 and observed-1 bits less [2] and [4]
+// (complete_expected_counts).
 inline constexpr float kFixScale = 1048576.0f;  // 2^20, class counts
 inline constexpr float kScoreScale = 65536.0f;  // 2^16, scores: a cell's
   // |log-likelihood| stays below 2^15 for any float alpha, beta (at most
   // 255 genes of |log p| <= 104), so each cell's term fits in 32 bits
+
+// E[n00] and E[n10] of a whole chain's sums (every cell counted once):
+// the dataset's observed-0 and observed-1 bits less E[n01] and E[n11].
+__device__ __forceinline__ void complete_expected_counts(const DatasetDev &ds,
+                                                         long long (&acc)[6]) {
+  acc[1] = (long long)(ds.sum_k - ds.sum_m) * 1048576ll - acc[2];
+  acc[3] = (long long)ds.sum_m * 1048576ll - acc[4];
+}
 
 // The warp's sum of an int64 per lane (|x| < 2^40) with three 32-bit
 // warp reductions: the high word and two 16-bit pieces of the low word,
@@ -1274,13 +1297,11 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
   for (int q = 0; q < Q; q++) {
     const int c = c0 + stride * q + lane;
     if (c >= n_cells) continue;
-    const float inv = 1.0f / z[q];
+    const float inv = __frcp_rn(z[q]);  // 1 / z, correctly rounded
     const float Ed = ed[q] * inv, Em = em[q] * inv;
-    const float pd = cb.pdb[q] - 8388608.0f, pm = cb.pmb[q] - 8388608.0f;
     acc[0] += (long long)__float2int_rn((r[q] + logf(z[q])) * kScoreScale);
-    acc[1] += (long long)__float2int_rn((pd - Ed) * kFixScale);  // E[n00]
+    // E[n00] and E[n10] follow from the chain's totals (class_sums)
     acc[2] += (long long)__float2int_rn(Ed * kFixScale);         // E[n01]
-    acc[3] += (long long)__float2int_rn((pm - Em) * kFixScale);  // E[n10]
     acc[4] += (long long)__float2int_rn(Em * kFixScale);         // E[n11]
     acc[5] += (long long)__float2int_rn(fmaf(mx[q], kLn2, r[q]) * kScoreScale);
   }
@@ -1357,8 +1378,10 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
       }
     }
   }
-#pragma unroll
-  for (int i = 0; i < 6; i++) acc[i] = warp_sum_ll(acc[i]);
+  acc[0] = warp_sum_ll(acc[0]);
+  acc[2] = warp_sum_ll(acc[2]);
+  acc[4] = warp_sum_ll(acc[4]);
+  acc[5] = warp_sum_ll(acc[5]);
 }
 
 // Max score with inherited counts (rows of up to four words, cells in

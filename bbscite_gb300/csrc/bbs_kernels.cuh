@@ -52,7 +52,7 @@ __host__ __device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n,
                                                      int w32, int q,
                                                      bool counts) {
   SlotSum o{};
-  uint8_t *p = slot + 4 * (2 * n * rs + 24 * wpc + 4);
+  uint8_t *p = slot + slot_head_bytes(n, rs, wpc);
   o.par0 = p;
   o.par1 = p + n;
   p += align16(2 * n) + wic * sum_warp_bytes(n, w32, q, counts);
@@ -148,6 +148,7 @@ __device__ __forceinline__ float evaluate(const uint32_t *rows, int n,
       for (int w = 0; w < wpc; w++)
         for (int i = 0; i < 6; i++) acc[i] += pp[6 * w + i];
     }
+    complete_expected_counts(ds, acc);
     sk = sm = 0;
 #pragma unroll
     for (int i = 0; i < 4; i++) e[i] = ll_to_float(acc[i + 1]) * (1.0f / kFixScale);
@@ -166,8 +167,8 @@ __device__ __forceinline__ void run_chain(
     ChainState *gstate,
     const bbs_raw_move *moves, bbs_step_trace *trace, int n_steps,
     const volatile int *cancel, int *status, uint32_t *buf0, uint32_t *buf1,
-    int *part, volatile int *sflag, const SlotSum &ss, Cells<W32, Q> &cb,
-    bool resident, int wpc, int wic, int lane) {
+    int *part, volatile int *sflag, uint4 *pbuf, const SlotSum &ss,
+    Cells<W32, Q> &cb, bool resident, int wpc, int wic, int lane) {
   const int n = ds.n_nodes;
   const bool multi = wpc > 1;
   const ChainState st = *gstate;
@@ -218,11 +219,17 @@ __device__ __forceinline__ void run_chain(
         break;
       }
     }
-    const uint64_t step = st.steps_done + (uint64_t)i;
+    // Philox blocks of the next 16 steps (a warp-uniform condition; the
+    // previous step's reads ended at its closing __syncwarp)
+    if (moves == nullptr && (i & 15) == 0) {
+      philox_fill(pbuf, md.seed, chain_id, st.steps_done + (uint64_t)i, lane);
+      __syncwarp();
+    }
     const bbs_raw_move raw =
-        moves != nullptr ? moves[i]
-                         : sample_move(md.mp, (uint32_t)n, md.seed, chain_id,
-                                       step, trace != nullptr);
+        moves != nullptr
+            ? moves[i]
+            : move_from_words(md.mp, (uint32_t)n, pbuf[2 * (i & 15)],
+                              pbuf[2 * (i & 15) + 1], trace != nullptr);
     const bool err_move = raw.move_type == BBS_MOVE_CHANGE_BETA;
     float palpha = alpha, pbeta = beta, pprior = prior;
     LogTable PL = L;
@@ -477,6 +484,8 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   uint32_t *buf1 = buf0 + n * RS;
   int *part = reinterpret_cast<int *>(buf0 + 2 * n * RS);
   volatile int *sflag = part + 24 * wpc;
+  uint4 *pbuf = reinterpret_cast<uint4 *>(
+      slot_base + 4 * (2 * n * RS + 24 * wpc + 4) + kPhiloxBytes * wic);
   Cells<W32, Q> cb;
   if (resident) load_cells<W32, Q>(cb, a.ds, 32 * wic, 32 * wpc, lane);
   SlotSum ss{};
@@ -507,7 +516,7 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
         K > 1 ? a.list_hash + (size_t)chain * K : nullptr,
         K > 1 ? a.list_beta + (size_t)chain * K : nullptr, K, a.states + chain,
         moves, trace,
-        a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, ss, cb,
+        a.n_steps, a.cancel, a.status, buf0, buf1, part, sflag, pbuf, ss, cb,
         resident, wpc, wic, lane);
   }
 }
@@ -519,7 +528,7 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
                                            const ModelDev &md, uint32_t chain,
                                            uint32_t d, uint32_t *buf0,
                                            int *part, volatile int *sflag,
-                                           const SlotSum &ss_in,
+                                           uint4 *pbuf, const SlotSum &ss_in,
                                            Cells<W32, Q> &cb, int lane) {
   constexpr int RS = rs_of_w32(W32);
   // the dataset's node count is within this launch's row width
@@ -536,7 +545,7 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
   run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
                          nullptr, nullptr, 1, b.states + chain, nullptr,
                          nullptr, b.n_steps, b.cancel, b.status, buf0, buf1,
-                         part, sflag, ss, cb, resident, 1, 0, lane);
+                         part, sflag, pbuf, ss, cb, resident, 1, 0, lane);
 }
 
 // Many datasets: warps take chains from a shared work list (costliest
@@ -558,6 +567,8 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
   volatile int *sflag = part + 24;
+  uint4 *pbuf = reinterpret_cast<uint4 *>(
+      slot_base + 4 * (2 * b.max_nodes * RS + 24 + 4));
   SlotSum ss{};
   if (scratch) {
     ss = slot_sum(slot_base, b.max_nodes, RS, 1, 0, W32, Q, counts);
@@ -590,12 +601,12 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
     // (measured faster there).
     if constexpr (SUM) {
       batch_unit<W32, Q, SUM>(b, b.ds[d], b.md[d], chain, d, buf0, part,
-                              sflag, ss, cb, lane);
+                              sflag, pbuf, ss, cb, lane);
     } else {
       const DatasetDev ds = b.ds[d];
       const ModelDev md = b.md[d];
-      batch_unit<W32, Q, SUM>(b, ds, md, chain, d, buf0, part, sflag, ss, cb,
-                              lane);
+      batch_unit<W32, Q, SUM>(b, ds, md, chain, d, buf0, part, sflag, pbuf,
+                              ss, cb, lane);
     }
   }
 }

@@ -25,12 +25,21 @@ __host__ __device__ inline int sum_warp_bytes(int n, int w32, int q,
          (counts && w32 <= 4 ? align16(pack_table_bytes(n, q)) : 0);
 }
 
-// One chain slot: two row buffers, the partial sums of both step parities
-// (2 x wpc x 12 words) and a flag word; with the scratch, the current and
-// proposed parent vectors and each warp's scratch.
+// Each warp's Philox blocks of 16 steps: 32 x 16 bytes.
+inline constexpr int kPhiloxBytes = 512;
+
+// The head of a chain slot: two row buffers, the partial sums of both step
+// parities (2 x wpc x 12 words), a flag word (16 bytes) and each warp's
+// Philox blocks.
+__host__ __device__ inline int slot_head_bytes(int n, int rs, int wpc) {
+  return 4 * (2 * n * rs + 24 * wpc + 4) + kPhiloxBytes * wpc;
+}
+
+// One chain slot: its head and, with the scratch, the current and proposed
+// parent vectors and each warp's scratch.
 __host__ __device__ inline int slot_bytes(int n, int rs, int wpc, bool scratch,
                                           int w32, int q, bool counts) {
-  int b = 4 * (2 * n * rs + 24 * wpc + 4);
+  int b = slot_head_bytes(n, rs, wpc);
   if (scratch) b += align16(2 * n) + wpc * sum_warp_bytes(n, w32, q, counts);
   return b;
 }

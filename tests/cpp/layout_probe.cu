@@ -3,7 +3,8 @@
 // 1..4 warps per chain (one-warp chains 1..8 per block), both scores.  For
 // each chain slot the pieces the kernels address -- the two row buffers,
 // both parities of the per-warp partial sums, the flag word, the parent
-// vectors, and each warp's node order, depth histogram and count table --
+// vectors, each warp's Philox blocks, node order, depth histogram and count
+// table --
 // must lie inside the slot, be disjoint and be aligned for their element
 // type; the block's increment tables (one per warp of a chain) must lie
 // after the slots and inside the launch's dynamic shared memory, and the
@@ -74,6 +75,11 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
     if ((sum ? part + psum : part + pmax) > flag)
       return fail("partials overrun the flag", n, q, wpc, cpb, sum, "");
     all.push_back({"flag", flag, flag + 4, 4});
+    // each warp's Philox blocks (32 x 16 bytes) after the flag words
+    for (int wic = 0; wic < wpc; wic++) {
+      const size_t ph = flag + 16 + (size_t)bbs::kPhiloxBytes * wic;
+      all.push_back({"philox", ph, ph + bbs::kPhiloxBytes, 16});
+    }
     if (scratch) {
       for (int wic = 0; wic < wpc; wic++) {
         const bbs::SlotSum ss =
