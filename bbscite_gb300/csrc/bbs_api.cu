@@ -1119,7 +1119,10 @@ int bbs_autotune(bbs_ctx *c, uint32_t probe_steps, float *best_ms) {
         if (wpc * q > groups + 1) continue;  // mostly empty cell slots
         for (int cpb : {1, 2, 4, 7, 8}) {
           if (wpc > 1 && cpb > 1) continue;
-          if (32 * cpb > chain_max_threads(q)) continue;
+          if (32 * wpc * cpb > chain_max_threads(q)) continue;
+          if (chain_launch_smem((int)c->n_nodes, (int)c->n_cells, q, wpc, cpb,
+                                c->md.score_mode != 0) > c->smem_block)
+            continue;  // too large a block
           c->q = q;
           c->wpc = wpc;
           c->cpb = cpb;
@@ -1762,6 +1765,7 @@ extern "C" int bbs_score_trees_noalloc(bbs_ctx *c, const uint64_t *dm_device,
 // ------------------------------------------------------------------------
 struct bbs_batch {
   int device = 0, n_sms = 0;
+  int smem_block = 0;  // dynamic shared memory a block may have (opt-in)
   cudaStream_t stream = nullptr;
   std::vector<cudaStream_t> side;  // one per launch group (graph branches)
   std::vector<cudaEvent_t> side_ev;
@@ -1926,9 +1930,45 @@ int batch_build_groups(bbs_batch *b) {
   return BBS_OK;
 }
 
+// Cells per lane of a launch group: 1 or 2 above 128 nodes.
+int group_q(const bbs_batch *b, const bbs_batch::Group &grp) {
+  return grp.w32 > 4 ? std::min(b->q, 2) : b->q;
+}
+
+// Whether the chains of a launch group inherit counts (one dataset whose
+// cells stay in registers, rows of up to four words).
+bool group_counts(const bbs_batch *b, const bbs_batch::Group &grp) {
+  return grp.only_ds >= 0 &&
+         inherits_counts(grp.w32, (int)b->n_cells[grp.only_ds],
+                         32 * group_q(b, grp));
+}
+
+// Whether every launch group of the current shape fits a block: its
+// threads within the kernel's bounds and its shared memory within the
+// device's limit.  Checked before a run launches anything.
+bool batch_shape_fits(const bbs_batch *b) {
+  for (const auto &grp : b->groups) {
+    const int q = group_q(b, grp);
+    if (32 * b->wpb > chain_max_threads(q)) return false;
+    const bool counts = group_counts(b, grp);
+    const int smem =
+        b->wpb * slot_bytes(grp.max_nodes, rs_of_w32(grp.w32), 1,
+                            b->sum || counts, grp.w32, q, counts) +
+        table_bytes(grp.max_nodes, grp.w32, q, 1, counts);
+    if (smem > b->smem_block) return false;
+  }
+  return true;
+}
+
 // Issues one run: zero the work counters, then one launch per group on its
 // own stream (forked from and joined back into b->stream).
 int batch_issue(bbs_batch *b, uint32_t n_steps) {
+  if (!batch_shape_fits(b))
+    return fail(BBS_ERR_SIZE,
+                "launch shape (%d cells per lane, %d warps per block) needs "
+                "more threads or shared memory per block than the kernel or "
+                "device allows",
+                b->q, b->wpb);
   BBS_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * kMaxW32,
                            b->stream), "memset");
   BBS_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(int) * kStatusWords, b->stream),
@@ -1956,9 +1996,8 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.status = b->d_status;
     a.max_nodes = grp.max_nodes;
     a.table_ds = grp.only_ds;
-    const int q = grp.w32 > 4 ? std::min(b->q, 2) : b->q;  // 1, 2 above 128 nodes
-    a.with_counts = grp.only_ds >= 0 &&
-                    inherits_counts(grp.w32, (int)b->n_cells[grp.only_ds], 32 * q);
+    const int q = group_q(b, grp);
+    a.with_counts = group_counts(b, grp) ? 1 : 0;
     const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");
     BBS_CUDA(cudaEventRecord(b->side_ev[g], b->side[g]), "event");
@@ -2008,6 +2047,8 @@ int bbs_batch_create(bbs_batch **out, uint32_t n_datasets,
     b->sum = sum;
     cudaGetDevice(&b->device);
     cudaDeviceGetAttribute(&b->n_sms, cudaDevAttrMultiProcessorCount, b->device);
+    cudaDeviceGetAttribute(&b->smem_block, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                           b->device);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
@@ -2243,6 +2284,7 @@ int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
           if (32 * wpb > chain_max_threads(q)) continue;
           int r = bbs_batch_set_launch(b, q, wpb, merge);
           if (r != BBS_OK) return r;
+          if (!batch_shape_fits(b)) continue;  // too large a block
           BBS_CUDA(cudaEventRecord(b->ev0, b->stream), "event");
           r = batch_issue(b, probe_steps);
           if (r != BBS_OK) return r;

@@ -915,8 +915,11 @@ typedef struct {
 
 /* cpu_scoring_benchmark/CPUTreeScorer.hpp:165-213 (AVX2 variant): for
  * every node, the maximum over cells of the four-class score over two
- * quadwords, summed over nodes. */
-static float orc_proxy_score(const float L[2][2], const uint64_t *mutq,
+ * quadwords, summed over nodes.  noipa: the compiler may not learn that
+ * the function is pure, so the benchmark's repeated scorings of a tree
+ * are not hoisted out of their loop and done once. */
+static float __attribute__((noipa)) orc_proxy_score(const float L[2][2],
+                                                    const uint64_t *mutq,
                              const uint64_t *knownq, const uint64_t *dm) {
   float tree_score = 0.0f;
   for (uint32_t node = 0; node < 128; node++) {
@@ -934,7 +937,7 @@ static float orc_proxy_score(const float L[2][2], const uint64_t *mutq,
           }
           s += (float)n * L[o][t];
         }
-      node_score = node_score > s ? node_score : s;
+      node_score = node_score < s ? s : node_score;  /* std::max(node_score, s) */
     }
     tree_score += node_score;
   }

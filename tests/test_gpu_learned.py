@@ -416,3 +416,29 @@ def test_sum_launch_shapes_give_identical_chains(native, G, Cn):
                                       t0["proposed_score"])
         np.testing.assert_array_equal(t["proposed_max_score"],
                                       t0["proposed_max_score"])
+
+
+@pytest.mark.parametrize("G,Cn", [(95, 96), (255, 80)])
+def test_autotune_skips_shapes_that_do_not_fit(native, G, Cn):
+    """One dataset whose chains inherit counts: some launch shapes of the
+    tuners' lists (8 warps of 4 cells per lane) need more shared memory
+    than a block may have.  Both tuners skip them, pick a shape that runs,
+    and leave the chains' states as they were."""
+    m, _, _ = D.generate_dataset(G * Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mut, known = D.matrix_to_bits(m)
+    p = _headline_params(native)
+    with native.Batch([(mut, known, Cn, G)], p) as b:
+        b.init_chains(64)
+        b.run(20)
+        before = b.save_chains()
+        assert b.autotune(16) > 0
+        assert b.save_chains() == before
+        b.run(20)
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(64)
+        c.run(20)
+        before = c.chains()
+        assert c.autotune(16) > 0
+        after = c.chains()
+        assert (after["dm"] == before["dm"]).all()
+        c.run(20)
