@@ -1207,10 +1207,20 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
       }
     }
   } else {
+    // the order entries one pair ahead: the rows' addresses are known when
+    // an iteration starts
+    uint32_t o0 = 0, o1 = 0;
+    if (i + 1 < n) {
+      o0 = sx.ord[i];
+      o1 = sx.ord[i + 1];
+    }
 #pragma unroll 1
     for (; i + 1 < n; i += 2) {
-      const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
       const int j0 = (int)(o0 & 0xFF), j1 = (int)(o1 & 0xFF);
+      if (i + 3 < n) {
+        o0 = sx.ord[i + 2];
+        o1 = sx.ord[i + 3];
+      }
       float2 fd[Q], fm[Q];
       uint32_t a[W32], b[W32];
       ld_row<W32>(rows + j0 * RS, a);
