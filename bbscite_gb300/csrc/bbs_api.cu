@@ -951,6 +951,18 @@ namespace {
 
 int start_run(bbs_ctx *c, uint32_t n_steps, const bbs_raw_move *d_moves,
               bbs_step_trace *d_trace) {
+  {
+    const int cpb = c->wpc > 1 ? 1 : c->cpb;
+    const int smem = chain_launch_smem((int)c->n_nodes, (int)c->n_cells, c->q,
+                                       c->wpc, cpb, c->md.score_mode != 0);
+    if (32 * c->wpc * cpb > chain_max_threads(c->q) || smem > c->smem_block)
+      return fail(BBS_ERR_SIZE,
+                  "launch shape (%d cells per lane, %d warps per chain, %d "
+                  "chains per block) needs %d bytes of shared memory and %d "
+                  "threads per block; the kernel and device allow %d and %d",
+                  c->q, c->wpc, cpb, smem, 32 * c->wpc * cpb, c->smem_block,
+                  chain_max_threads(c->q));
+  }
   RunArgs a{};
   a.ds = c->ds;
   a.md = c->md;

@@ -236,7 +236,8 @@ def test_batch_autotune_and_shapes_agree(native):
         datasets.append((mut, known, Cn, G))
     p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=3)
     results = []
-    for shape in ((1, 1, 0), (2, 4, 0), (4, 2, 1), None):
+    for shape in ((1, 1, 0), (2, 4, 0), (4, 2, 1), (3, 8, 0), (4, 7, 1),
+                  None):
         with native.Batch(datasets, p) as b:
             b.init_chains(4)
             if shape is None:
@@ -392,7 +393,8 @@ def test_sum_launch_shapes_give_identical_chains(native, G, Cn):
     m, _, _ = D.generate_dataset(G + 5 * Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
     mut, known = D.matrix_to_bits(m)
     shapes = [(3, 1, 4), (1, 1, 1), (2, 1, 2), (1, 2, 1), (1, 3, 1),
-              (2, 2, 1), (1, 4, 1), (4, 1, 1), (4, 2, 1)]
+              (2, 2, 1), (1, 4, 1), (4, 1, 1), (4, 2, 1), (3, 1, 7),
+              (3, 1, 8)]
     qmax = 2 if G + 1 > 128 else 4
     outs = []
     for q, wpc, cpb in shapes:
@@ -402,7 +404,14 @@ def test_sum_launch_shapes_give_identical_chains(native, G, Cn):
         with native.Context(mut, known, Cn, G, p) as c:
             c.init_chains(9)
             c.set_launch(q, wpc, cpb)
-            tr = c.run(150, trace=True)
+            try:
+                tr = c.run(150, trace=True)
+            except native.BbsError as e:
+                # a block too large for this shape's shared memory is
+                # refused before anything runs
+                assert e.code == native.BBS_ERR_SIZE, e
+                assert q >= 3 and cpb >= 7, e
+                continue
             outs.append((c.chains(), c.best(), tr))
     ch0, b0, t0 = outs[0]
     for ch, b, t in outs[1:]:
