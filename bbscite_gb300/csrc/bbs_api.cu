@@ -1947,6 +1947,13 @@ int group_q(const bbs_batch *b, const bbs_batch::Group &grp) {
   return grp.w32 > 4 ? std::min(b->q, 2) : b->q;
 }
 
+// Warps per block of a launch group: the batch's, within the kernel's
+// bounds for the group's cells per lane (groups of more than 128 nodes
+// take at most 2 cells per lane and so at most 4 warps per block).
+int group_wpb(const bbs_batch *b, const bbs_batch::Group &grp) {
+  return std::min(b->wpb, chain_max_threads(group_q(b, grp)) / 32);
+}
+
 // Whether the chains of a launch group inherit counts (one dataset whose
 // cells stay in registers, rows of up to four words).
 bool group_counts(const bbs_batch *b, const bbs_batch::Group &grp) {
@@ -1955,16 +1962,16 @@ bool group_counts(const bbs_batch *b, const bbs_batch::Group &grp) {
                          32 * group_q(b, grp));
 }
 
-// Whether every launch group of the current shape fits a block: its
-// threads within the kernel's bounds and its shared memory within the
-// device's limit.  Checked before a run launches anything.
+// Whether every launch group of the current shape fits a block: its shared
+// memory within the device's limit (threads are clamped to the kernel's
+// bounds by group_wpb).  Checked before a run launches anything.
 bool batch_shape_fits(const bbs_batch *b) {
   for (const auto &grp : b->groups) {
     const int q = group_q(b, grp);
-    if (32 * b->wpb > chain_max_threads(q)) return false;
+    const int wpb = group_wpb(b, grp);
     const bool counts = group_counts(b, grp);
     const int smem =
-        b->wpb * slot_bytes(grp.max_nodes, rs_of_w32(grp.w32), 1,
+        wpb * slot_bytes(grp.max_nodes, rs_of_w32(grp.w32), 1,
                             b->sum || counts, grp.w32, q, counts) +
         table_bytes(grp.max_nodes, grp.w32, q, 1, counts);
     if (smem > b->smem_block) return false;
@@ -1981,6 +1988,10 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
                 "more threads or shared memory per block than the kernel or "
                 "device allows",
                 b->q, b->wpb);
+  // one work counter per launch group (one group per row width)
+  if (b->groups.size() > (size_t)kMaxW32)
+    return fail(BBS_ERR_STATE, "%zu launch groups, at most %d", b->groups.size(),
+                kMaxW32);
   BBS_CUDA(cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * kMaxW32,
                            b->stream), "memset");
   BBS_CUDA(cudaMemsetAsync(b->d_status, 0, sizeof(int) * kStatusWords, b->stream),
@@ -2010,7 +2021,8 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.table_ds = grp.only_ds;
     const int q = group_q(b, grp);
     a.with_counts = group_counts(b, grp) ? 1 : 0;
-    const int e = launch_batch(a, grp.w32, q, b->sum, b->wpb, b->n_sms, b->side[g]);
+    const int e = launch_batch(a, grp.w32, q, b->sum, group_wpb(b, grp),
+                               b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");
     BBS_CUDA(cudaEventRecord(b->side_ev[g], b->side[g]), "event");
     BBS_CUDA(cudaStreamWaitEvent(b->stream, b->side_ev[g], 0), "wait");

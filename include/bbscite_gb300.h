@@ -316,8 +316,9 @@ BBS_API int bbs_batch_init_chains(bbs_batch *batch, uint32_t chains_per_dataset)
 BBS_API int bbs_batch_run(bbs_batch *batch, uint32_t n_steps);
 BBS_API int bbs_batch_last_run_ms(const bbs_batch *batch, float *ms);
 /* Launch shape: cells per lane (1-4; 1-2 above 128 nodes) and warps per
- * block (1-4, or 1-8 with 3-4 cells per lane; a run with a larger block
- * fails);
+ * block (1-8; a launch group with 1-2 cells per lane takes at most 4, and
+ * a block too large for its shared memory fails the run with
+ * BBS_ERR_SIZE);
  * merge_rows != 0 runs 1- and 3-word trees with their 2- and 4-word row
  * stride group (one launch per group instead of two). */
 BBS_API int bbs_batch_set_launch(bbs_batch *batch, int cells_per_lane,

@@ -226,15 +226,25 @@ def test_batch_equals_single_dataset_runs(native, score, move):
         assert (bests[d]["dm"] == want["dm"]).all()
 
 
-def test_batch_autotune_and_shapes_agree(native):
-    rng = np.random.default_rng(10)
+@pytest.mark.parametrize("score", ["max", "sum"])
+def test_batch_autotune_and_shapes_agree(native, score):
+    """Every launch shape of the batched form -- cells per lane, warps per
+    block, merged row widths -- and the tuned one give the same chains, and
+    every chain of every launch group runs all its steps."""
+    # every row width of up to four words with 1-4 groups of 32 cells, and
+    # two wider datasets
+    specs = [(G, Cn) for G in (20, 50, 80, 110) for Cn in (20, 50, 80, 110)]
+    specs += [(200, 40), (160, 300)]
     datasets = []
-    for i in range(12):
-        G, Cn = int(rng.integers(16, 128)), int(rng.integers(16, 256))
+    for i, (G, Cn) in enumerate(specs):
         m, _, _ = D.generate_dataset(500 + i, G, Cn, 1e-3, 0.2, 0.1, 0.0)
         mut, known = D.matrix_to_bits(m)
         datasets.append((mut, known, Cn, G))
-    p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=3)
+    nd = len(datasets)
+    if score == "max":
+        p = native.default_params(alpha_mean=1e-3, beta_mean=0.2, seed=3)
+    else:
+        p = _headline_params(native, seed=3)
     results = []
     for shape in ((1, 1, 0), (2, 4, 0), (4, 2, 1), (3, 8, 0), (4, 7, 1),
                   None):
@@ -245,9 +255,18 @@ def test_batch_autotune_and_shapes_agree(native):
             else:
                 b.set_launch(*shape)
             b.run(150)
-            results.append([b.best(d)["score"] for d in range(12)])
+            img = b.save_chains()
+            # every chain ran: its state (128 bytes, at the image's end)
+            # counts 150 steps
+            states = np.frombuffer(img[-128 * 4 * nd:], dtype=np.uint8)
+            steps = states.reshape(4 * nd, 128)[:, 80:88].copy().view(
+                np.uint64).ravel()
+            assert (steps == 150).all(), (shape, steps)
+            results.append(([b.best(d)["score"] for d in range(nd)],
+                            img[-128 * 4 * nd:]))
     for r in results[1:]:
-        assert r == results[0]
+        assert r[0] == results[0][0]
+        assert r[1] == results[0][1]  # the last chain states, byte for byte
 
 
 def test_langevin_learns_alpha(native):
