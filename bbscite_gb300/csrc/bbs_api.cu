@@ -1954,9 +1954,12 @@ int group_wpb(const bbs_batch *b, const bbs_batch::Group &grp) {
   return std::min(b->wpb, chain_max_threads(group_q(b, grp)) / 32);
 }
 
-// Whether the chains of a launch group inherit counts (one dataset whose
-// cells stay in registers, rows of up to four words).
+// Whether the chains of a launch group inherit counts: rows of up to four
+// words when the group has one dataset whose cells stay in registers (the
+// block's increment table holds that dataset's cells); wider rows always
+// (each warp builds its gene table from the cells it scores).
 bool group_counts(const bbs_batch *b, const bbs_batch::Group &grp) {
+  if (grp.w32 > 4) return true;
   return grp.only_ds >= 0 &&
          inherits_counts(grp.w32, (int)b->n_cells[grp.only_ds],
                          32 * group_q(b, grp));

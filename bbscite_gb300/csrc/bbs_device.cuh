@@ -825,6 +825,12 @@ struct SumCtx {
   const uint32_t *inc;  // [n][32][NW]: per-gene packed increments of the
                         // warp's cells, or null
   const uint8_t *par;   // parent vector of the evaluated tree, or null
+  // Rows of five to eight words (inherited counts without a table of every
+  // node): the packed counts of the last kRing order positions (position i
+  // in entry i % kRing) and the gene table of the cells being scored, or
+  // null.
+  uint32_t *ring;       // [kRing][32][NW]
+  uint32_t *gt;         // [ceil(n / 8)][32][NW]
 };
 
 // ord and hist of the tree with ancestor rows `rows`; the parent of each
@@ -891,6 +897,135 @@ __device__ __forceinline__ void canonical_order(const uint32_t *rows, int n,
     if (valid && (same & below) == 0) hist[dep[g]] += __popc(same);
     __syncwarp();
   }
+}
+
+// The canonical order for counts inherited through a ring (rows of five to
+// eight words): the positions of canonical_order, each entry node | ppos
+// << 8 with ppos the order position of the node's parent, from `par`, the
+// tree's parent vector (the root, at position 0, gets 0).  Returns whether
+// every node lies fewer than kRing positions after its parent, so that the
+// parent's counts are still in the ring when the node is reached; where
+// not, ord still holds the canonical node order in its low bytes.  hist
+// doubles as the node -> position map (32 ceil(n / 32) >= n ints).
+template <int W32>
+__device__ __forceinline__ bool ring_order(const uint32_t *rows, int n,
+                                           const uint8_t *par, uint16_t *ord,
+                                           int *hist, int lane) {
+  constexpr int RS = rs_of_w32(W32);
+  const int B = (n + 31) >> 5;
+  for (int i = lane; i < 32 * B; i += 32) hist[i] = 0;
+  __syncwarp();
+  int dep[W32], at[W32];
+#pragma unroll
+  for (int g = 0; g < W32; g++) {
+    const int x = 32 * g + lane;
+    dep[g] = -1;
+    at[g] = 0;
+    if (x < n) {
+      uint32_t a[W32];
+      ld_row<W32>(rows + x * RS, a);
+      int pc = 0;
+#pragma unroll
+      for (int k = 0; k < W32; k++) pc += __popc(a[k]);
+      dep[g] = pc - 1;
+      atomicAdd(&hist[pc - 1], 1);
+    }
+  }
+  __syncwarp();
+  int loc[W32], s = 0;
+#pragma unroll
+  for (int k = 0; k < W32; k++) {
+    loc[k] = k < B ? hist[lane * B + k] : 0;
+    s += loc[k];
+  }
+  int incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(BBS_FULL_MASK, incl, o);
+    if (lane >= o) incl += v;
+  }
+  int run = incl - s;
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < W32; k++)
+    if (k < B) {
+      hist[lane * B + k] = run;
+      run += loc[k];
+    }
+  __syncwarp();
+  const unsigned below = (1u << lane) - 1u;
+#pragma unroll
+  for (int g = 0; g < W32; g++) {
+    const int x = 32 * g + lane;
+    const bool valid = x < n;
+    const unsigned same = __match_any_sync(BBS_FULL_MASK, valid ? dep[g] : -1);
+    if (valid) at[g] = hist[dep[g]] + __popc(same & below);
+    __syncwarp();
+    if (valid && (same & below) == 0) hist[dep[g]] += __popc(same);
+    __syncwarp();
+  }
+  // node -> position, then the entries with their parents' positions
+#pragma unroll
+  for (int g = 0; g < W32; g++) {
+    const int x = 32 * g + lane;
+    if (x < n) hist[x] = at[g];
+  }
+  __syncwarp();
+  bool ok = true;
+#pragma unroll
+  for (int g = 0; g < W32; g++) {
+    const int x = 32 * g + lane;
+    if (x < n) {
+      const int pp = x == n - 1 ? 0 : hist[min((int)par[x], n - 1)];
+      ord[at[g]] = (uint16_t)(x | (pp << 8));
+      ok = ok && at[g] - pp < kRing;
+    }
+  }
+  __syncwarp();
+  return __all_sync(BBS_FULL_MASK, ok);
+}
+
+// The gene table of the lane's Q cells (layout in bbs_layout.h): gene j's
+// increment of every cell is then (entry >> (j & 7)) & 0x01010101, word by
+// word.  Each lane writes, and later reads, only its own column.
+template <int W32, int Q>
+__device__ __forceinline__ void build_gene_table(const Cells<W32, Q> &cb,
+                                                 uint32_t *gt, int n,
+                                                 int lane) {
+  constexpr int NW = kPackWords<Q>;
+#pragma unroll
+  for (int w = 0; w < W32; w++) {
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int g8 = 4 * w + b;
+      if (8 * g8 < n) {
+        // byte b of D, then byte b of M, in the two low bytes
+        const uint32_t sel = (uint32_t)b | ((uint32_t)(4 + b) << 4);
+        uint32_t y[NW];
+#pragma unroll
+        for (int h = 0; h < NW; h++) {
+          constexpr int top = Q - 1;
+          const int qa = 2 * h, qb = 2 * h + 1 < Q ? 2 * h + 1 : top;
+          const uint32_t lo = __byte_perm(cb.D[qa][w], cb.M[qa][w], sel);
+          const uint32_t hi = 2 * h + 1 < Q
+                                  ? __byte_perm(cb.D[qb][w], cb.M[qb][w], sel)
+                                  : 0u;
+          y[h] = __byte_perm(lo, hi, 0x5410u);
+        }
+        st_pack<Q>(gt, g8 * 32 + lane, y);
+      }
+    }
+  }
+}
+
+// Gene j's packed increments of the lane's cells, from the gene table.
+template <int Q>
+__device__ __forceinline__ void gene_inc(const uint32_t *gt, int j, int lane,
+                                         uint32_t (&g)[kPackWords<Q>]) {
+  ld_pack<Q>(gt, (j >> 3) * 32 + lane, g);
+  const uint32_t sh = (uint32_t)j & 7u;
+#pragma unroll
+  for (int w = 0; w < kPackWords<Q>; w++) g[w] = (g[w] >> sh) & 0x01010101u;
 }
 
 // The parent vector of the tree with ancestor rows `rows`: each node's
@@ -1039,6 +1174,83 @@ __device__ __forceinline__ void inherit_one(const SumCtx &sx, int i, int lane,
   st_pack<Q>(sx.cnt, j * 32 + lane, k);
 }
 
+// inherit_pair for rows of five to eight words: the parents' counts come
+// from the ring (entries hold the parents' order positions, ring_order),
+// the increments from the gene table, and positions i and i + 1 are stored
+// in the ring.
+template <int Q, int NW = kPackWords<Q>>
+__device__ __forceinline__ void inherit_pair_ring(const SumCtx &sx, int i,
+                                                  int lane,
+                                                  uint32_t (&k0)[NW],
+                                                  uint32_t (&k1)[NW], int &j0,
+                                                  int &j1) {
+  const uint32_t o0 = sx.ord[i], o1 = sx.ord[i + 1];
+  j0 = (int)(o0 & 0xFF);
+  j1 = (int)(o1 & 0xFF);
+  const int p0 = (int)(o0 >> 8), p1 = (int)(o1 >> 8);
+  uint32_t a0[NW], a1[NW], g0[NW], g1[NW];
+  ld_pack<Q>(sx.ring, (p0 & (kRing - 1)) * 32 + lane, a0);
+  ld_pack<Q>(sx.ring, (p1 & (kRing - 1)) * 32 + lane, a1);
+  gene_inc<Q>(sx.gt, j0, lane, g0);
+  gene_inc<Q>(sx.gt, j1, lane, g1);
+#pragma unroll
+  for (int w = 0; w < NW; w++) {
+    k0[w] = a0[w] + g0[w];
+    k1[w] = (p1 == i ? k0[w] : a1[w]) + g1[w];
+  }
+  st_pack<Q>(sx.ring, (i & (kRing - 1)) * 32 + lane, k0);
+  st_pack<Q>(sx.ring, ((i + 1) & (kRing - 1)) * 32 + lane, k1);
+}
+
+template <int Q, int NW = kPackWords<Q>>
+__device__ __forceinline__ void inherit_one_ring(const SumCtx &sx, int i,
+                                                 int lane, uint32_t (&k)[NW],
+                                                 int &j) {
+  const uint32_t o = sx.ord[i];
+  j = (int)(o & 0xFF);
+  const int p = (int)(o >> 8);
+  uint32_t a[NW], g[NW];
+  ld_pack<Q>(sx.ring, (p & (kRing - 1)) * 32 + lane, a);
+  gene_inc<Q>(sx.gt, j, lane, g);
+#pragma unroll
+  for (int w = 0; w < NW; w++) k[w] = a[w] + g[w];
+  st_pack<Q>(sx.ring, (i & (kRing - 1)) * 32 + lane, k);
+}
+
+// The two count sources by inheritance: the table of every node (rows of
+// up to four words) or the ring.
+template <int Q, bool RING, int NW = kPackWords<Q>>
+__device__ __forceinline__ void inherit2(const SumCtx &sx, int i, int lane,
+                                         uint32_t (&k0)[NW],
+                                         uint32_t (&k1)[NW], int &j0,
+                                         int &j1) {
+  if constexpr (RING)
+    inherit_pair_ring<Q>(sx, i, lane, k0, k1, j0, j1);
+  else
+    inherit_pair<Q>(sx, i, lane, k0, k1, j0, j1);
+}
+
+template <int Q, bool RING, int NW = kPackWords<Q>>
+__device__ __forceinline__ void inherit1(const SumCtx &sx, int i, int lane,
+                                         uint32_t (&k)[NW], int &j) {
+  if constexpr (RING)
+    inherit_one_ring<Q>(sx, i, lane, k, j);
+  else
+    inherit_one<Q>(sx, i, lane, k, j);
+}
+
+// The root's zero counts, at order position 0.
+template <int Q, bool RING, int NW = kPackWords<Q>>
+__device__ __forceinline__ void store_root(const SumCtx &sx, int lane) {
+  uint32_t zero[NW];
+#pragma unroll
+  for (int w = 0; w < NW; w++) zero[w] = 0u;
+  if constexpr (RING)
+    st_pack<Q>(sx.ring, lane, zero);
+  else
+    st_pack<Q>(sx.cnt, (int)(sx.ord[0] & 0xFF) * 32 + lane, zero);
+}
+
 // The sum score's float work of two nodes, side by side in the halves of
 // paired registers, for the lane's Q cells: t = base + d c1 + m c2, its
 // power of two, the running maximum of t, and the sums of 2^t, 2^t d and
@@ -1099,6 +1311,11 @@ struct QF {
 };
 
 template <int Q>
+struct QI {
+  int v[Q];
+};
+
+template <int Q>
 struct Resum {
   QF<Q> z, ed, em;
 };
@@ -1144,13 +1361,38 @@ __device__ __noinline__ Resum<Q> resum_cells(const uint32_t *rows, int n,
   return o;
 }
 
-template <int W32, int Q, bool INHERIT>
+// resum_cells on cells it loads itself (c = c0 + stride q + lane).
+template <int W32, int Q>
+__device__ __noinline__ Resum<Q> resum_cells_reload(
+    const uint32_t *rows, int n, const DatasetDev *ds, int c0, int stride,
+    const SumCtx sx, int lane, float c1, float c2, const QF<Q> base,
+    unsigned bad) {
+  Cells<W32, Q> cb;
+  load_cells<W32, Q>(cb, *ds, c0, stride, lane);
+  return resum_cells<W32, Q, false>(rows, n, cb, sx, lane, c1, c2, base, bad);
+}
+
+// Lane sums of k and m at the chosen nodes of cells it loads itself.
+template <int W32, int Q>
+__device__ __noinline__ int2 counts_at_reload(const uint32_t *rows,
+                                              const DatasetDev *ds, int c0,
+                                              int stride, const QI<Q> bj,
+                                              int lane) {
+  Cells<W32, Q> cb;
+  load_cells<W32, Q>(cb, *ds, c0, stride, lane);
+  int k = 0, m = 0;
+  counts_at<W32, Q>(rows, cb, bj.v, k, m);
+  return make_int2(k, m);
+}
+
+template <int W32, int Q, bool INHERIT, bool RING = false>
 __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const Cells<W32, Q> &cb,
                                           const LogTable &L, int c0, int stride,
                                           int lane, int n_cells,
                                           long long (&acc)[6],
-                                          const SumCtx &sx) {
+                                          const SumCtx &sx,
+                                          const DatasetDev *ds = nullptr) {
   constexpr int RS = rs_of_w32(W32);
   constexpr int NW = kPackWords<Q>;
   const float c1 = (L.l01 - L.l00) * kLog2E;  // per counted observed-0 bit
@@ -1167,12 +1409,7 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     base2[q] = dup2(base[q]);
   }
   // the root (ord[0]) has no counted bits: t = base
-  if constexpr (INHERIT) {
-    uint32_t zero[NW];
-#pragma unroll
-    for (int w = 0; w < NW; w++) zero[w] = 0u;
-    st_pack<Q>(sx.cnt, (int)(sx.ord[0] & 0xFF) * 32 + lane, zero);
-  }
+  if constexpr (INHERIT) store_root<Q, RING>(sx, lane);
 #pragma unroll
   for (int q = 0; q < Q; q++) {
     mx[q] = base[q];
@@ -1188,16 +1425,16 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     if (i + 1 < n) {
       uint32_t kA0[NW], kA1[NW], kB0[NW], kB1[NW];
       int jA0, jA1, jB0, jB1;  // node numbers (the max score uses them)
-      inherit_pair<Q>(sx, i, lane, kA0, kA1, jA0, jA1);
+      inherit2<Q, RING>(sx, i, lane, kA0, kA1, jA0, jA1);
 #pragma unroll 1
       for (; i + 5 < n; i += 4) {
-        inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+        inherit2<Q, RING>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
         sum_counts2<Q, NW>(kA0, kA1, c1p, c2p, base2, mx, z2, ed2, em2);
-        inherit_pair<Q>(sx, i + 4, lane, kA0, kA1, jA0, jA1);
+        inherit2<Q, RING>(sx, i + 4, lane, kA0, kA1, jA0, jA1);
         sum_counts2<Q, NW>(kB0, kB1, c1p, c2p, base2, mx, z2, ed2, em2);
       }
       if (i + 3 < n) {
-        inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+        inherit2<Q, RING>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
         sum_counts2<Q, NW>(kA0, kA1, c1p, c2p, base2, mx, z2, ed2, em2);
         sum_counts2<Q, NW>(kB0, kB1, c1p, c2p, base2, mx, z2, ed2, em2);
         i += 4;
@@ -1242,7 +1479,7 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
     if constexpr (INHERIT) {
       uint32_t k[NW];
       int j;
-      inherit_one<Q>(sx, i, lane, k, j);
+      inherit1<Q, RING>(sx, i, lane, k, j);
 #pragma unroll
       for (int q = 0; q < Q; q++) {
         fd[q] = pack_d_biased(k[q >> 1], q) - 8388608.0f;
@@ -1293,8 +1530,16 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
       }
       b2.v[q] = base[q];
     }
-    const Resum<Q> o = resum_cells<W32, Q, INHERIT>(rows, n, cb, sx, lane,
-                                                           c1, c2, b2, badm);
+    // (the ring no longer holds every node: masked popcounts of the cells,
+    // which the ring path reloads so that their rows need no registers
+    // during the node loop)
+    Resum<Q> o;
+    if constexpr (RING)
+      o = resum_cells_reload<W32, Q>(rows, n, ds, c0, stride, sx, lane, c1,
+                                     c2, b2, badm);
+    else
+      o = resum_cells<W32, Q, INHERIT>(rows, n, cb, sx, lane, c1, c2, b2,
+                                       badm);
 #pragma unroll
     for (int q = 0; q < Q; q++)
       if (bad[q]) {
@@ -1321,11 +1566,11 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
 // warp-reduced), its terms added in the canonical order (sx.ord, built
 // here).  Inherited counts serve cells held in registers when sx brings the
 // parent vector, the count table and the increment table.
-// The masked-popcount node loop for rows of up to four words, out of line:
-// there it serves only streamed cells and mixed launch groups, and keeping
-// one copy of it outside the chain kernels leaves the inherited-count loop
-// and the step code small.  Wider rows have no other loop and keep it
-// inline.
+// The masked-popcount node loop, out of line: it serves only streamed cells
+// and mixed launch groups (rows of up to four words), trees whose order
+// does not fit the ring or whose parent vector is not known (wider rows),
+// and keeping one copy of it outside the chain kernels leaves the
+// inherited-count loops and the step code small.
 struct Acc6 {
   long long v[6];
 };
@@ -1353,7 +1598,33 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
                                          const SumCtx &sx) {
 #pragma unroll
   for (int i = 0; i < 6; i++) acc[i] = 0;
-  canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
+  if constexpr (W32 > 4) {
+    // rows of five to eight words: counts through the ring where the
+    // tree's parent vector is known and its order fits the ring, the cells
+    // streamed in chunks with a gene table built per chunk
+    bool ring = false;
+    if (sx.ring != nullptr && sx.par != nullptr)
+      ring = ring_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
+    else
+      canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
+    if (ring) {
+      const int span = 32 * wpc * Q;
+      for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
+        Cells<W32, Q> cc;
+        load_cells<W32, Q>(cc, ds, c0 + 32 * wic, 32 * wpc, lane);
+        build_gene_table<W32, Q>(cc, sx.gt, n, lane);
+        sum_cells<W32, Q, true, true>(rows, n, cc, L, c0 + 32 * wic, 32 * wpc,
+                                      lane, ds.n_cells, acc, sx, &ds);
+      }
+      acc[0] = warp_sum_ll(acc[0]);
+      acc[2] = warp_sum_ll(acc[2]);
+      acc[4] = warp_sum_ll(acc[4]);
+      acc[5] = warp_sum_ll(acc[5]);
+      return;
+    }
+  } else {
+    canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
+  }
   if (resident) {
     bool inherit = false;
     if constexpr (W32 <= 4)
@@ -1363,29 +1634,19 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
         sum_cells<W32, Q, true>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
                                 ds.n_cells, acc, sx);
     } else {
-      if constexpr (W32 <= 4) {
-        const Acc6 o = sum_cells_popc<W32, Q>(rows, n, cb, L, 32 * wic,
-                                              32 * wpc, lane, ds.n_cells, sx);
+      const Acc6 o = sum_cells_popc<W32, Q>(rows, n, cb, L, 32 * wic,
+                                            32 * wpc, lane, ds.n_cells, sx);
 #pragma unroll
-        for (int k = 0; k < 6; k++) acc[k] += o.v[k];
-      } else {
-        sum_cells<W32, Q, false>(rows, n, cb, L, 32 * wic, 32 * wpc, lane,
-                                 ds.n_cells, acc, sx);
-      }
+      for (int k = 0; k < 6; k++) acc[k] += o.v[k];
     }
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
       load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      if constexpr (W32 <= 4) {
-        const Acc6 o = sum_cells_popc<W32, Q>(rows, n, cb, L, c0 + 32 * wic,
-                                              32 * wpc, lane, ds.n_cells, sx);
+      const Acc6 o = sum_cells_popc<W32, Q>(rows, n, cb, L, c0 + 32 * wic,
+                                            32 * wpc, lane, ds.n_cells, sx);
 #pragma unroll
-        for (int k = 0; k < 6; k++) acc[k] += o.v[k];
-      } else {
-        sum_cells<W32, Q, false>(rows, n, cb, L, c0 + 32 * wic, 32 * wpc,
-                                 lane, ds.n_cells, acc, sx);
-      }
+      for (int k = 0; k < 6; k++) acc[k] += o.v[k];
     }
   }
   acc[0] = warp_sum_ll(acc[0]);
@@ -1429,11 +1690,13 @@ __device__ __forceinline__ void max_update2(const uint32_t (&k0)[NW], int j0,
   }
 }
 
-template <int W32, int Q>
-__device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb,
+template <int W32, int Q, bool RING = false>
+__device__ __forceinline__ void max_cells_inherit(const uint32_t *rows, int n,
+                                                  const Cells<W32, Q> &cb,
                                                   const LogTable &L, float nz,
                                                   int lane, const SumCtx &sx,
-                                                  int &k, int &m) {
+                                                  int &k, int &m,
+                                                  QI<Q> *chosen = nullptr) {
   constexpr int NW = kPackWords<Q>;
   const LogTable2 L2 = log_table2(L, nz);
   float best[Q];
@@ -1441,10 +1704,7 @@ __device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb
   float2 pdb[Q], pmb[Q];
   {
     const int root = (int)(sx.ord[0] & 0xFF);
-    uint32_t zero[NW];
-#pragma unroll
-    for (int w = 0; w < NW; w++) zero[w] = 0u;
-    st_pack<Q>(sx.cnt, root * 32 + lane, zero);
+    store_root<Q, RING>(sx, lane);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
       best[q] = pair_score(0, 0, cb.pdb[q], cb.pmb[q], L.l00, L.l01, L.l10,
@@ -1458,16 +1718,16 @@ __device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb
   if (i + 1 < n) {
     uint32_t kA0[NW], kA1[NW], kB0[NW], kB1[NW];
     int jA0, jA1, jB0, jB1;
-    inherit_pair<Q>(sx, i, lane, kA0, kA1, jA0, jA1);
+    inherit2<Q, RING>(sx, i, lane, kA0, kA1, jA0, jA1);
 #pragma unroll 1
     for (; i + 5 < n; i += 4) {
-      inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+      inherit2<Q, RING>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
       max_update2<Q, NW>(kA0, jA0, kA1, jA1, pdb, pmb, L2, best, bj);
-      inherit_pair<Q>(sx, i + 4, lane, kA0, kA1, jA0, jA1);
+      inherit2<Q, RING>(sx, i + 4, lane, kA0, kA1, jA0, jA1);
       max_update2<Q, NW>(kB0, jB0, kB1, jB1, pdb, pmb, L2, best, bj);
     }
     if (i + 3 < n) {
-      inherit_pair<Q>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
+      inherit2<Q, RING>(sx, i + 2, lane, kB0, kB1, jB0, jB1);
       max_update2<Q, NW>(kA0, jA0, kA1, jA1, pdb, pmb, L2, best, bj);
       max_update2<Q, NW>(kB0, jB0, kB1, jB1, pdb, pmb, L2, best, bj);
       i += 4;
@@ -1479,7 +1739,7 @@ __device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb
   if (i < n) {
     uint32_t kk[NW];
     int j;
-    inherit_one<Q>(sx, i, lane, kk, j);
+    inherit1<Q, RING>(sx, i, lane, kk, j);
 #pragma unroll
     for (int q = 0; q < Q; q++) {
       const float s = pair_score_b(pack_d_biased(kk[q >> 1], q),
@@ -1488,15 +1748,37 @@ __device__ __forceinline__ void max_cells_inherit(int n, const Cells<W32, Q> &cb
       max_select(s, j, best[q], bj[q]);
     }
   }
-  // the counts at the chosen nodes: k = popc(K & A) = d + m
+  // the counts at the chosen nodes: k = popc(K & A) = d + m (the ring no
+  // longer holds every node: the caller takes masked popcounts then)
+  if constexpr (RING) {
 #pragma unroll
-  for (int q = 0; q < Q; q++) {
-    uint32_t c[NW];
-    ld_pack<Q>(sx.cnt, bj[q] * 32 + lane, c);
-    const uint32_t f = pack_field<NW>(c, q);
-    k += (int)(f & 0xFFu) + (int)(f >> 8);
-    m += (int)(f >> 8);
+    for (int q = 0; q < Q; q++) chosen->v[q] = bj[q];
+  } else {
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      uint32_t c[NW];
+      ld_pack<Q>(sx.cnt, bj[q] * 32 + lane, c);
+      const uint32_t f = pack_field<NW>(c, q);
+      k += (int)(f & 0xFFu) + (int)(f >> 8);
+      m += (int)(f >> 8);
+    }
   }
+}
+
+// The max score's masked-popcount pass over one chunk of cells it loads
+// itself: lane sums of k and m at the chosen nodes.
+template <int W32, int Q>
+__device__ __noinline__ int2 max_chunk_popc(const uint32_t *rows, int n,
+                                            const DatasetDev *ds, int c0,
+                                            int stride, const LogTable L,
+                                            int lane) {
+  Cells<W32, Q> cb;
+  load_cells<W32, Q>(cb, *ds, c0, stride, lane);
+  int bj[Q], k = 0, m = 0;
+  best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, ds->neg_zero,
+                     bj);
+  counts_at<W32, Q>(rows, cb, bj, k, m);
+  return make_int2(k, m);
 }
 
 // This warp's part of the class sums over its cells (max score).  Cells
@@ -1510,6 +1792,31 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
                                            int wic, int lane, int &sk,
                                            int &sm, const SumCtx &sx) {
   int k = 0, m = 0, bj[Q];
+  if constexpr (W32 > 4) {
+    // rows of five to eight words: counts through the ring, as for the sum
+    // score
+    if (sx.ring != nullptr && sx.par != nullptr &&
+        ring_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane)) {
+      const int span = 32 * wpc * Q;
+      for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
+        QI<Q> chosen;
+        {
+          Cells<W32, Q> cc;
+          load_cells<W32, Q>(cc, ds, c0 + 32 * wic, 32 * wpc, lane);
+          build_gene_table<W32, Q>(cc, sx.gt, n, lane);
+          max_cells_inherit<W32, Q, true>(rows, n, cc, L, ds.neg_zero, lane,
+                                          sx, k, m, &chosen);
+        }
+        const int2 km = counts_at_reload<W32, Q>(rows, &ds, c0 + 32 * wic,
+                                                 32 * wpc, chosen, lane);
+        k += km.x;
+        m += km.y;
+      }
+      sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);
+      sm = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)m);
+      return;
+    }
+  }
   bool inherit = false;
   if constexpr (W32 <= 4)
     inherit = resident && sx.cnt != nullptr && sx.inc != nullptr &&
@@ -1517,7 +1824,8 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
   if (inherit) {
     if constexpr (W32 <= 4) {
       canonical_order<W32>(rows, n, sx.par, sx.ord, sx.hist, lane);
-      max_cells_inherit<W32, Q>(n, cb, L, ds.neg_zero, lane, sx, k, m);
+      max_cells_inherit<W32, Q>(rows, n, cb, L, ds.neg_zero, lane, sx, k,
+                                  m);
     }
   } else if (resident) {
     best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, ds.neg_zero, bj);
@@ -1525,9 +1833,18 @@ __device__ __forceinline__ void score_part(const uint32_t *rows, int n,
   } else {
     const int span = 32 * wpc * Q;
     for (int c0 = 0; c0 < ds.n_cells; c0 += span) {
-      load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
-      best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11, ds.neg_zero, bj);
-      counts_at<W32, Q>(rows, cb, bj, k, m);
+      if constexpr (W32 > 4) {
+        // (out of line: wider rows take their counts through the ring)
+        const int2 km = max_chunk_popc<W32, Q>(rows, n, &ds, c0 + 32 * wic,
+                                               32 * wpc, L, lane);
+        k += km.x;
+        m += km.y;
+      } else {
+        load_cells<W32, Q>(cb, ds, c0 + 32 * wic, 32 * wpc, lane);
+        best_nodes<W32, Q>(rows, n, cb, L.l00, L.l01, L.l10, L.l11,
+                           ds.neg_zero, bj);
+        counts_at<W32, Q>(rows, cb, bj, k, m);
+      }
     }
   }
   sk = (int)__reduce_add_sync(BBS_FULL_MASK, (uint32_t)k);

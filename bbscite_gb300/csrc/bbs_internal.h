@@ -21,13 +21,19 @@ __host__ __device__ constexpr int rs_of_w32(int w32) {
   return 2 * ((w32 + 1) / 2);
 }
 __host__ __device__ constexpr int w32_of_nodes(int n) { return (n + 31) / 32; }
-// Chains inherit counts from the parent (max or sum score) when their rows
-// have up to four words and all their cells stay in registers (at most
-// cells_per_pass = 32 x cells per lane x warps per chain): the increment
-// tables and each warp's count table exist then.
+// Chains inherit counts from the parent (max or sum score):
+//   - rows of up to four words, when all their cells stay in registers (at
+//     most cells_per_pass = 32 x cells per lane x warps per chain): the
+//     block's increment tables and each warp's count table of every node
+//     exist then;
+//   - rows of five to eight words, always: each warp keeps a ring of the
+//     counts of the last kRing nodes in the canonical order and a gene
+//     table of the cells it is scoring, rebuilt per chunk of streamed
+//     cells.
+inline constexpr int kRing = 64;
 __host__ __device__ constexpr bool inherits_counts(int w32, int n_cells,
                                                    int cells_per_pass) {
-  return w32 <= 4 && n_cells <= cells_per_pass;
+  return w32 > 4 || n_cells <= cells_per_pass;
 }
 
 // Cumulative move thresholds and jump sd (src/RawMoveDistribution.hpp:

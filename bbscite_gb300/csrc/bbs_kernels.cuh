@@ -61,6 +61,10 @@ __host__ __device__ __forceinline__ SlotSum slot_sum(uint8_t *slot, int n,
   o.sx.hist = reinterpret_cast<int *>(p);
   p += align16(4 * 32 * ((n + 31) / 32));
   if (counts && w32 <= 4) o.sx.cnt = reinterpret_cast<uint32_t *>(p);
+  if (counts && w32 > 4) {
+    o.sx.ring = reinterpret_cast<uint32_t *>(p);
+    o.sx.gt = reinterpret_cast<uint32_t *>(p + align16(ring_bytes(q)));
+  }
   return o;
 }
 
@@ -182,16 +186,18 @@ __device__ __forceinline__ void run_chain(
   // when floor(u * count) reaches the count) changes the rows in a way the
   // parent-vector form does not follow, and may leave rows that are no tree.
   // Such trees are scored with masked popcounts, which take any rows.
+  // Rows of five to eight words inherit through the ring, which needs the
+  // parent vectors too (any cells, resident or streamed).
   uint8_t *cpar = nullptr, *ppar = nullptr;
   bool cur_par_ok = false;  // cpar describes cur
-  if constexpr (W32 <= 4) {
-    if (ss.sx.inc != nullptr && resident) {
-      cpar = ss.par0;
-      ppar = ss.par1;
-      if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
-      if (multi) __syncthreads(); else __syncwarp();
-      cur_par_ok = parents_match_rows<W32>(cur, n, cpar, lane);
-    }
+  const bool track = W32 <= 4 ? ss.sx.inc != nullptr && resident
+                              : ss.sx.ring != nullptr;
+  if (track) {
+    cpar = ss.par0;
+    ppar = ss.par1;
+    if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
+    if (multi) __syncthreads(); else __syncwarp();
+    cur_par_ok = parents_match_rows<W32>(cur, n, cpar, lane);
   }
   SumCtx sx = ss.sx;
   float alpha = st.alpha, beta = st.beta, score = st.score, prior = st.prior;
@@ -290,23 +296,21 @@ __device__ __forceinline__ void run_chain(
     // every one and record a mismatch outside that case as a failed device
     // check.
     bool par_ok = false;
-    if constexpr (W32 <= 4) {
-      if (cpar != nullptr && cur_par_ok) {
-        const bool suspect = scored != cur && fallback_move;
-        bool check = suspect;
+    if (cpar != nullptr && cur_par_ok) {
+      const bool suspect = scored != cur && fallback_move;
+      bool check = suspect;
 #ifdef BBS_CHECKED
-        check = true;
+      check = true;
 #endif
-        par_ok = true;
-        if (check) {
-          par_ok = parents_match_rows<W32>(scored, n,
-                                           scored == cur ? cpar : ppar, lane);
+      par_ok = true;
+      if (check) {
+        par_ok = parents_match_rows<W32>(scored, n,
+                                         scored == cur ? cpar : ppar, lane);
 #ifdef BBS_CHECKED
-          if (!suspect)
-            device_check(par_ok, status, kCheckParent,
-                         (uint32_t)raw.move_type, 4u);
+        if (!suspect)
+          device_check(par_ok, status, kCheckParent,
+                       (uint32_t)raw.move_type, 4u);
 #endif
-        }
       }
     }
     sx.par = par_ok ? (scored == cur ? cpar : ppar) : nullptr;
@@ -396,15 +400,13 @@ __device__ __forceinline__ void run_chain(
         uint8_t *tp = cpar;
         cpar = ppar;
         ppar = tp;
-        if constexpr (W32 <= 4) {
-          cur_par_ok = prop_par_ok;
-          if (cpar != nullptr && !cur_par_ok) {
-            // the new tree's own parent vector, where its rows are a tree
-            if (multi) __syncthreads(); else __syncwarp();
-            if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
-            if (multi) __syncthreads(); else __syncwarp();
-            cur_par_ok = parents_match_rows<W32>(cur, n, cpar, lane);
-          }
+        cur_par_ok = prop_par_ok;
+        if (cpar != nullptr && !cur_par_ok) {
+          // the new tree's own parent vector, where its rows are a tree
+          if (multi) __syncthreads(); else __syncwarp();
+          if (wic == 0) derive_parents<W32>(cur, n, cpar, ss.sx.hist, lane);
+          if (multi) __syncthreads(); else __syncwarp();
+          cur_par_ok = parents_match_rows<W32>(cur, n, cpar, lane);
         }
       }
       alpha = palpha;
@@ -474,7 +476,9 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   const int cpb = wpb / wpc;
   const int slot = wib / wpc, wic = wib - slot * wpc;
   const int n = a.ds.n_nodes;
-  const bool resident = a.ds.n_cells <= 32 * wpc * Q;
+  // rows of five to eight words stream their cells per evaluation (their
+  // counts come through the ring and a gene table built per chunk)
+  const bool resident = W32 <= 4 && a.ds.n_cells <= 32 * wpc * Q;
   // the same decisions as the launcher's, for the whole block
   const bool counts = inherits_counts(W32, a.ds.n_cells, 32 * wpc * Q);
   const bool scratch = SUM || counts;
@@ -533,7 +537,9 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
   constexpr int RS = rs_of_w32(W32);
   // the dataset's node count is within this launch's row width
   uint32_t *buf1 = buf0 + ds.n_nodes * RS;
-  const bool resident = ds.n_cells <= 32 * Q;
+  // rows of five to eight words stream their cells per evaluation (their
+  // counts come through the ring and a gene table built per chunk)
+  const bool resident = W32 <= 4 && ds.n_cells <= 32 * Q;
   if (resident) load_cells<W32, Q>(cb, ds, 0, 32, lane);
   const uint64_t off = b.chain_off[chain];
   // Philox key: the chain's number within its dataset, so a dataset's

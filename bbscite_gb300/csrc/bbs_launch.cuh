@@ -50,8 +50,8 @@ int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   const int threads = 32 * wpb;
   if (threads > chain_max_threads(Q)) return (int)cudaErrorInvalidConfiguration;
   const bool counts = b.with_counts != 0;
-  if (counts && (W32 > 4 || b.table_ds < 0))
-    return (int)cudaErrorInvalidValue;  // counts need one dataset's rows
+  if (counts && W32 <= 4 && b.table_ds < 0)
+    return (int)cudaErrorInvalidValue;  // count tables need one dataset's rows
   const size_t smem =
       (size_t)wpb * slot_bytes(b.max_nodes, RS, 1, SUM || counts, W32, Q,
                                counts) +

@@ -15,14 +15,30 @@ __host__ __device__ inline int pack_table_bytes(int n, int q) {
 // Shared memory of the chain kernels, in bytes (16-byte aligned pieces).
 __host__ __device__ inline int align16(int b) { return (b + 15) & ~15; }
 
+// Rows of five to eight words: a warp's ring of the packed counts of the
+// last kRing nodes in the canonical order, and its gene table, one entry
+// of NW words per 8 genes and lane laid out as the counts are packed (word
+// h: byte 0 the D bits of the 8 genes for cell slot 2h, byte 1 their M
+// bits, bytes 2 and 3 the same for cell slot 2h + 1).
+__host__ __device__ inline int ring_bytes(int q) {
+  return 4 * ((q + 1) / 2) * kRing * 32;
+}
+__host__ __device__ inline int gene_table_bytes(int n, int q) {
+  return 4 * ((q + 1) / 2) * ((n + 7) / 8) * 32;
+}
+
 // Per warp of a chain with the node-order scratch (every sum-score chain:
 // its order is canonical; every chain that inherits counts): the canonical
 // node order, its depth histogram and, with `counts`, the packed counts of
-// every node for the lane's cells.
+// every node for the lane's cells (rows of up to four words) or the ring
+// and gene table (wider rows).
 __host__ __device__ inline int sum_warp_bytes(int n, int w32, int q,
                                               bool counts) {
-  return align16(2 * n) + align16(4 * 32 * ((n + 31) / 32)) +
-         (counts && w32 <= 4 ? align16(pack_table_bytes(n, q)) : 0);
+  int b = align16(2 * n) + align16(4 * 32 * ((n + 31) / 32));
+  if (counts)
+    b += w32 <= 4 ? align16(pack_table_bytes(n, q))
+                  : align16(ring_bytes(q)) + align16(gene_table_bytes(n, q));
+  return b;
 }
 
 // Each warp's Philox blocks of 16 steps: 32 x 16 bytes.

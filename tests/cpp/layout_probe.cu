@@ -4,7 +4,7 @@
 // each chain slot the pieces the kernels address -- the two row buffers,
 // both parities of the per-warp partial sums, the flag word, the parent
 // vectors, each warp's Philox blocks, node order, depth histogram and count
-// table --
+// table (or ring and gene table) --
 // must lie inside the slot, be disjoint and be aligned for their element
 // type; the block's increment tables (one per warp of a chain) must lie
 // after the slots and inside the launch's dynamic shared memory, and the
@@ -42,18 +42,21 @@ void add_table(std::vector<Piece> &all, const char *name, size_t w, int n,
 }
 
 // One launch: cpb slots of wpc warps, the tables after them.  `counts`
-// says whether the chains inherit counts (rows of up to four words, cells
-// in registers): the slots then carry count tables and the launch its
-// increment tables.
+// says whether the chains inherit counts: with rows of up to four words
+// (cells in registers) the slots then carry count tables and the launch its
+// increment tables; with wider rows (always) each warp carries a ring of
+// kRing entries and a gene table of ceil(n / 8) entries.
 bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
   const int w32 = bbs::w32_of_nodes(n);
   const int rs = bbs::rs_of_w32(w32);
-  if (w32 > 4) counts = false;
   const bool scratch = sum || counts;
   const int sb = bbs::slot_bytes(n, rs, wpc, scratch, w32, q, counts);
   const size_t tb = (size_t)bbs::table_bytes(n, w32, q, wpc, counts);
   const size_t total = (size_t)cpb * sb + tb;
-  if (w32 <= 4 && (size_t)bbs::chain_launch_smem(n, counts ? 32 * wpc * q : 32 * wpc * q + 1, q, wpc, cpb, sum) != total)
+  // the launchers' size, for the cell counts that give this `counts`
+  const int cells = counts ? 32 * wpc * q : 32 * wpc * q + 1;
+  if (bbs::inherits_counts(w32, cells, 32 * wpc * q) == counts &&
+      (size_t)bbs::chain_launch_smem(n, cells, q, wpc, cpb, sum) != total)
     return fail("launch size differs from chain_launch_smem", n, q, wpc, cpb,
                 sum, "");
   std::vector<uint8_t> smem(total + 16);
@@ -98,11 +101,19 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
         if (hist < (size_t)4 * n)
           return fail("histogram smaller than n ints", n, q, wpc, cpb, sum, "");
         all.push_back({"hist", off(ss.sx.hist), off(ss.sx.hist) + hist, 4});
-        if (counts) {
-          if (ss.sx.cnt == nullptr)
+        if (counts && w32 <= 4) {
+          if (ss.sx.cnt == nullptr || ss.sx.ring != nullptr)
             return fail("no count table", n, q, wpc, cpb, sum, "");
           add_table(all, "cnt", off(ss.sx.cnt), n, q);
-        } else if (ss.sx.cnt != nullptr) {
+        } else if (counts) {
+          if (ss.sx.ring == nullptr || ss.sx.gt == nullptr ||
+              ss.sx.cnt != nullptr)
+            return fail("no ring or gene table", n, q, wpc, cpb, sum, "");
+          // entries [kRing][32] and [ceil(n / 8)][32], packed like counts
+          add_table(all, "ring", off(ss.sx.ring), bbs::kRing, q);
+          add_table(all, "gene table", off(ss.sx.gt), (n + 7) / 8, q);
+        } else if (ss.sx.cnt != nullptr || ss.sx.ring != nullptr ||
+                   ss.sx.gt != nullptr) {
           return fail("count table without inherited counts", n, q, wpc,
                       cpb, sum, "");
         }
@@ -112,7 +123,7 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
       if (all[i].lo < o || all[i].hi > o + sb)
         return fail("piece outside its slot", n, q, wpc, cpb, sum, all[i].name);
   }
-  if (counts) {
+  if (counts && w32 <= 4) {
     const size_t lo = (size_t)cpb * sb;
     if (tb != (size_t)wpc * bbs::inc_table_bytes(n, q))
       return fail("increment tables sized wrongly", n, q, wpc, cpb, sum, "");

@@ -368,6 +368,34 @@ def test_inherited_count_chains_replay_in_fp64(native, orc, G, Cn, q, move,
                       final["dm"][ch]) <= 2
 
 
+@pytest.mark.parametrize("G,Cn,launch", [(200, 150, (1, 1, 2)),
+                                         (255, 300, (2, 1, 4)),
+                                         (255, 300, (2, 2, 1))])
+def test_wide_row_ring_chains_replay_in_fp64(native, orc, G, Cn, launch):
+    """Sum-score chains with learned rates and rows of five to eight words:
+    counts through the ring of the last 64 nodes in the canonical order,
+    the cells streamed in chunks with a gene table per chunk.  Two chains
+    start from star trees, whose order does not fit the ring (masked
+    popcounts score them until the moves deepen the tree); every step of
+    every chain is replayed in FP64."""
+    m, _, _ = D.generate_dataset(3000 + G, G, Cn, 5e-4, 0.25, 0.08, 0.01)
+    mut, known = D.matrix_to_bits(m)
+    p = _headline_params(native, "langevin", 0.1, seed=0x51DE + G)
+    chains, steps = 3, 200
+    rng = np.random.default_rng(G + 3 * Cn)
+    star = np.full(G + 1, G, dtype=np.uint32)
+    starts = np.stack([star, star, D.random_parent_vector(rng, G)])
+    with native.Context(mut, known, Cn, G, p) as c:
+        c.init_chains(chains, starts)
+        c.set_launch(*launch)
+        tr = c.run(steps, trace=True)
+        final = c.chains()
+    assert int(tr["accepted"].sum()) > 0
+    for ch in range(chains):
+        assert replay(orc, native, m, p, starts[ch], tr[ch],
+                      final["dm"][ch]) <= 2
+
+
 def test_headline_batch_equals_replayed_chains(native, orc):
     """The batched launch of the bench's headline shape -- one 95 x 96
     dataset, 3 cells per lane, 4-warp blocks, the dataset's increment table
@@ -403,12 +431,13 @@ def test_headline_batch_equals_replayed_chains(native, orc):
                       final["dm"][ch]) <= 2
 
 
-@pytest.mark.parametrize("G,Cn", [(95, 96), (40, 200), (127, 64)])
+@pytest.mark.parametrize("G,Cn", [(95, 96), (40, 200), (127, 64), (200, 150)])
 def test_sum_launch_shapes_give_identical_chains(native, G, Cn):
     """Sum-score chains with learned rates are bit-identical under every
     launch shape: inherited counts (cells in registers, one or several
-    warps per chain) and masked popcounts (streamed cells) add the same
-    terms in the same order."""
+    warps per chain; for 200 genes the ring, over chunks of 32 to 256
+    cells) and masked popcounts (streamed cells) add the same terms in the
+    same order."""
     m, _, _ = D.generate_dataset(G + 5 * Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
     mut, known = D.matrix_to_bits(m)
     shapes = [(3, 1, 4), (1, 1, 1), (2, 1, 2), (1, 2, 1), (1, 3, 1),

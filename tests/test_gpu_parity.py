@@ -211,11 +211,13 @@ def test_apply_moves_fuzz(native, orc, G):
 # -------------------------------------------------------------- chains --
 
 def _replay_check(native, orc, m, alpha, beta, start_parents, raws,
-                  exact_scores=True):
+                  exact_scores=True, launch=None):
     c, mut, known = ctx_for(native, m, alpha, beta)
     n_chains, n_steps = raws.shape
     with c:
         c.init_chains(n_chains, np.stack(start_parents))
+        if launch is not None:
+            c.set_launch(*launch)
         tr = c.run(n_steps, moves=np.ascontiguousarray(raws).view(
             native.RAW_MOVE), trace=True)
         final = c.chains()
@@ -264,6 +266,32 @@ def test_mcmc_replay_random(native, orc, G, Cn, chains):
                      for ch in range(chains)])
     starts = [D.random_parent_vector(rng, G) for _ in range(chains)]
     _replay_check(native, orc, m, 1e-3, 0.2, starts, raws)
+
+
+@pytest.mark.parametrize("G,Cn,launch", [(200, 150, (1, 1, 3)),
+                                         (255, 300, (2, 1, 2)),
+                                         (255, 300, (2, 3, 1))])
+def test_wide_rows_replay_with_stars_and_node0_fallbacks(native, orc, G, Cn,
+                                                         launch):
+    """Rows of five to eight words take their counts through a ring of the
+    last 64 nodes in the canonical order.  Chains started from star trees
+    (every gene a child of the root: the order does not fit the ring, so
+    masked popcounts score them until the moves deepen the tree), and moves
+    whose k-th (non)descendant falls back to node 0 (u = 1.0: those
+    proposals' parent vectors are checked against their rows), replay bit
+    for bit against the oracle: decisions, class counts, scores and final
+    rows, with one and with several warps per chain."""
+    rng = np.random.default_rng(G * 7 + Cn)
+    m, _, _ = D.generate_dataset(G + Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
+    mp = orc.move_probs(0.0, 0.55, 0.4, 0.05)
+    steps, chains = 300, 3
+    raws = np.stack([orc.sample_moves(mp, G + 1, 41, ch, steps)
+                     for ch in range(chains)])
+    raws["raw_descendant_of_v"][rng.random(raws.shape) < 0.03] = 1.0
+    raws["raw_nondescendant_of_v"][rng.random(raws.shape) < 0.03] = 1.0
+    star = np.full(G + 1, G, dtype=np.uint32)
+    starts = [star, star.copy(), D.random_parent_vector(rng, G)]
+    _replay_check(native, orc, m, 1e-3, 0.2, starts, raws, launch=launch)
 
 
 @pytest.fixture(scope="module")
