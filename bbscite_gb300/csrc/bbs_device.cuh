@@ -1361,15 +1361,42 @@ __device__ __noinline__ Resum<Q> resum_cells(const uint32_t *rows, int n,
   return o;
 }
 
-// resum_cells on cells it loads itself (c = c0 + stride q + lane).
-template <int W32, int Q>
-__device__ __noinline__ Resum<Q> resum_cells_reload(
-    const uint32_t *rows, int n, const DatasetDev *ds, int c0, int stride,
-    const SumCtx sx, int lane, float c1, float c2, const QF<Q> base,
-    unsigned bad) {
-  Cells<W32, Q> cb;
-  load_cells<W32, Q>(cb, *ds, c0, stride, lane);
-  return resum_cells<W32, Q, false>(rows, n, cb, sx, lane, c1, c2, base, bad);
+// resum_cells for the ring: the counts inherited once more along the
+// order (the chunk's gene table is still in place), the same terms summed
+// in the same order as resum_cells, so the sums are those of the other
+// count sources.
+template <int Q>
+__device__ __noinline__ Resum<Q> resum_cells_ring(int n, const SumCtx sx,
+                                                  int lane, float c1,
+                                                  float c2, const QF<Q> base,
+                                                  unsigned bad) {
+  constexpr int NW = kPackWords<Q>;
+  Resum<Q> o;
+#pragma unroll
+  for (int q = 0; q < Q; q++) o.z.v[q] = o.ed.v[q] = o.em.v[q] = 0.0f;
+  store_root<Q, true>(sx, lane);
+#pragma unroll 1
+  for (int i2 = 0; i2 < n; i2++) {
+    uint32_t k[NW];
+    if (i2 == 0) {
+#pragma unroll
+      for (int w = 0; w < NW; w++) k[w] = 0u;
+    } else {
+      int j;
+      inherit_one_ring<Q>(sx, i2, lane, k, j);
+    }
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      if (!((bad >> q) & 1u)) continue;
+      const float fd = pack_d_biased(k[q >> 1], q) - 8388608.0f;
+      const float fm = pack_m_biased(k[q >> 1], q) - 8388608.0f;
+      const float e = ex2_approx(fmaf(fd, c1, fmaf(fm, c2, base.v[q])));
+      o.z.v[q] += e;
+      o.ed.v[q] = fmaf(e, fd, o.ed.v[q]);
+      o.em.v[q] = fmaf(e, fm, o.em.v[q]);
+    }
+  }
+  return o;
 }
 
 // Lane sums of k and m at the chosen nodes of cells it loads itself.
@@ -1391,8 +1418,7 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
                                           const LogTable &L, int c0, int stride,
                                           int lane, int n_cells,
                                           long long (&acc)[6],
-                                          const SumCtx &sx,
-                                          const DatasetDev *ds = nullptr) {
+                                          const SumCtx &sx) {
   constexpr int RS = rs_of_w32(W32);
   constexpr int NW = kPackWords<Q>;
   const float c1 = (L.l01 - L.l00) * kLog2E;  // per counted observed-0 bit
@@ -1530,13 +1556,11 @@ __device__ __forceinline__ void sum_cells(const uint32_t *rows, int n,
       }
       b2.v[q] = base[q];
     }
-    // (the ring no longer holds every node: masked popcounts of the cells,
-    // which the ring path reloads so that their rows need no registers
-    // during the node loop)
+    // (the ring no longer holds every node: the counts are inherited once
+    // more)
     Resum<Q> o;
     if constexpr (RING)
-      o = resum_cells_reload<W32, Q>(rows, n, ds, c0, stride, sx, lane, c1,
-                                     c2, b2, badm);
+      o = resum_cells_ring<Q>(n, sx, lane, c1, c2, b2, badm);
     else
       o = resum_cells<W32, Q, INHERIT>(rows, n, cb, sx, lane, c1, c2, b2,
                                        badm);
@@ -1614,7 +1638,7 @@ __device__ __forceinline__ void sum_part(const uint32_t *rows, int n,
         load_cells<W32, Q>(cc, ds, c0 + 32 * wic, 32 * wpc, lane);
         build_gene_table<W32, Q>(cc, sx.gt, n, lane);
         sum_cells<W32, Q, true, true>(rows, n, cc, L, c0 + 32 * wic, 32 * wpc,
-                                      lane, ds.n_cells, acc, sx, &ds);
+                                      lane, ds.n_cells, acc, sx);
       }
       acc[0] = warp_sum_ll(acc[0]);
       acc[2] = warp_sum_ll(acc[2]);

@@ -556,9 +556,14 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
 
 // Many datasets: warps take chains from a shared work list (costliest
 // first); each chain brings its own dataset and rules.  One warp per chain.
+// Rows of five to eight words leave the register count free (up to 255):
+// a one-warp slot there takes about 31 KB of shared memory, so at most 7
+// such blocks fit an SM whatever their registers, and with the tighter
+// bound of two cells per lane (168) the sum score's kernel spilled
+// (measured at 255 x 512: 7.5 M against 6.7 M chain-steps/s).
 template <int W32, int Q, bool SUM>
 __global__ void __launch_bounds__(ChainBounds<Q>::threads,
-                                  ChainBounds<Q>::min_blocks)
+                                  W32 > 4 ? 1 : ChainBounds<Q>::min_blocks)
     batch_kernel(const BatchArgs b) {
   extern __shared__ __align__(16) uint32_t smem[];
   constexpr int RS = rs_of_w32(W32);

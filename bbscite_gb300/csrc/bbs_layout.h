@@ -76,6 +76,8 @@ __host__ __device__ inline int table_bytes(int n, int w32, int q, int wpc,
 // at 16, 12 and 8 resident warps per SM for 1, 2 and 3-4 cells per lane
 // (registers per thread 128, 168, 255), in blocks of up to 4, 4 and 8
 // warps: eight warps of three or four cells per lane fill an SM alone.
+// (The batched kernel for rows of five to eight words takes up to 255
+// registers: shared memory limits those launches first.)
 inline constexpr int kMaxBlockThreads = 256;
 __host__ __device__ constexpr int chain_max_threads(int q) {
   return q >= 3 ? 256 : 128;
