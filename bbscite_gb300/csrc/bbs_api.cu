@@ -1812,6 +1812,7 @@ struct bbs_batch {
   unsigned int *d_counters = nullptr;
   int *d_status = nullptr;
   int q = 2, wpb = 4, merge = 0;
+  int wpc = 1;  // warps per chain (above 1 a block is one chain)
   // graph of the current shape and step count
   cudaGraphExec_t graph = nullptr;
   uint32_t graph_steps = 0;
@@ -1947,22 +1948,24 @@ int group_q(const bbs_batch *b, const bbs_batch::Group &grp) {
   return grp.w32 > 4 ? std::min(b->q, 2) : b->q;
 }
 
-// Warps per block of a launch group: the batch's, within the kernel's
-// bounds for the group's cells per lane (groups of more than 128 nodes
-// take at most 2 cells per lane and so at most 4 warps per block).
+// Warps per block of a launch group: with one-warp chains the batch's,
+// within the kernel's bounds for the group's cells per lane (groups of
+// more than 128 nodes take at most 2 cells per lane and so at most 4 warps
+// per block); with several warps per chain the chain's (one per block).
 int group_wpb(const bbs_batch *b, const bbs_batch::Group &grp) {
+  if (b->wpc > 1) return b->wpc;
   return std::min(b->wpb, chain_max_threads(group_q(b, grp)) / 32);
 }
 
 // Whether the chains of a launch group inherit counts: rows of up to four
 // words when the group has one dataset whose cells stay in registers (the
-// block's increment table holds that dataset's cells); wider rows always
+// block's increment tables hold that dataset's cells); wider rows always
 // (each warp builds its gene table from the cells it scores).
 bool group_counts(const bbs_batch *b, const bbs_batch::Group &grp) {
   if (grp.w32 > 4) return true;
   return grp.only_ds >= 0 &&
          inherits_counts(grp.w32, (int)b->n_cells[grp.only_ds],
-                         32 * group_q(b, grp));
+                         32 * b->wpc * group_q(b, grp));
 }
 
 // Whether every launch group of the current shape fits a block: its shared
@@ -1971,12 +1974,12 @@ bool group_counts(const bbs_batch *b, const bbs_batch::Group &grp) {
 bool batch_shape_fits(const bbs_batch *b) {
   for (const auto &grp : b->groups) {
     const int q = group_q(b, grp);
-    const int wpb = group_wpb(b, grp);
+    const int slots = group_wpb(b, grp) / b->wpc;
     const bool counts = group_counts(b, grp);
     const int smem =
-        wpb * slot_bytes(grp.max_nodes, rs_of_w32(grp.w32), 1,
-                            b->sum || counts, grp.w32, q, counts) +
-        table_bytes(grp.max_nodes, grp.w32, q, 1, counts);
+        slots * slot_bytes(grp.max_nodes, rs_of_w32(grp.w32), b->wpc,
+                           b->sum || counts, grp.w32, q, counts) +
+        table_bytes(grp.max_nodes, grp.w32, q, b->wpc, counts);
     if (smem > b->smem_block) return false;
   }
   return true;
@@ -2024,6 +2027,7 @@ int batch_issue(bbs_batch *b, uint32_t n_steps) {
     a.table_ds = grp.only_ds;
     const int q = group_q(b, grp);
     a.with_counts = group_counts(b, grp) ? 1 : 0;
+    a.wpc = b->wpc;
     const int e = launch_batch(a, grp.w32, q, b->sum, group_wpb(b, grp),
                                b->n_sms, b->side[g]);
     if (e != 0) return cuda_fail(e, "batch kernel launch");
@@ -2286,6 +2290,22 @@ int bbs_batch_get_launch(const bbs_batch *b, int *q, int *wpb, int *merge) {
   return BBS_OK;
 }
 
+int bbs_batch_set_chain_warps(bbs_batch *b, int warps_per_chain) {
+  if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
+  if (warps_per_chain < 1 || warps_per_chain > 4)
+    return fail(BBS_ERR_INPUT, "warps per chain must be 1, 2, 3 or 4");
+  b->wpc = warps_per_chain;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  return BBS_OK;
+}
+
+int bbs_batch_get_chain_warps(const bbs_batch *b, int *warps_per_chain) {
+  if (!b || !warps_per_chain) return fail(BBS_ERR_INPUT, "NULL argument");
+  *warps_per_chain = b->wpc;
+  return BBS_OK;
+}
+
 int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
   try {
     if (!b) return fail(BBS_ERR_INPUT, "NULL batch");
@@ -2304,12 +2324,21 @@ int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
     BBS_CUDA(cp(sbst.p, b->d_best, rb), "save");
     BBS_CUDA(cp(sst.p, b->d_states, sb), "save");
     float best = 1e30f;
-    int bq = b->q, bw = b->wpb, bm = b->merge;
+    int bq = b->q, bw = b->wpb, bm = b->merge, bc = b->wpc;
+    // one-warp chains in blocks of 1-8, or one chain of 2 or 4 warps per
+    // block (warps per block then = warps per chain)
+    struct Shape {
+      int wpb, wpc;
+    };
+    const Shape shapes[] = {{1, 1}, {2, 1}, {4, 1}, {7, 1}, {8, 1},
+                            {2, 2}, {4, 4}};
     for (int merge : {0, 1})
       for (int q : {1, 2, 3, 4})
-        for (int wpb : {1, 2, 4, 7, 8}) {
-          if (32 * wpb > chain_max_threads(q)) continue;
-          int r = bbs_batch_set_launch(b, q, wpb, merge);
+        for (const Shape &sh : shapes) {
+          if (32 * sh.wpb > chain_max_threads(q)) continue;
+          int r = bbs_batch_set_launch(b, q, sh.wpb, merge);
+          if (r != BBS_OK) return r;
+          r = bbs_batch_set_chain_warps(b, sh.wpc);
           if (r != BBS_OK) return r;
           if (!batch_shape_fits(b)) continue;  // too large a block
           BBS_CUDA(cudaEventRecord(b->ev0, b->stream), "event");
@@ -2322,14 +2351,16 @@ int bbs_batch_autotune(bbs_batch *b, uint32_t probe_steps, float *best_ms) {
           if (ms < best) {
             best = ms;
             bq = q;
-            bw = wpb;
+            bw = sh.wpb;
             bm = merge;
+            bc = sh.wpc;
           }
           BBS_CUDA(cp(b->d_rows, sr.p, rb), "restore");
           BBS_CUDA(cp(b->d_best, sbst.p, rb), "restore");
           BBS_CUDA(cp(b->d_states, sst.p, sb), "restore");
         }
-    const int r = bbs_batch_set_launch(b, bq, bw, bm);
+    int r = bbs_batch_set_launch(b, bq, bw, bm);
+    if (r == BBS_OK) r = bbs_batch_set_chain_warps(b, bc);
     BBS_CUDA(cudaStreamSynchronize(b->stream), "restore");
     if (best_ms) *best_ms = best;
     return r;

@@ -128,8 +128,11 @@ struct BatchArgs {
   int table_ds;              // the launch's only dataset, or -1
   int with_counts;           // 1: the chains inherit counts (rows of up to
                              // four words, one dataset whose cells stay in
-                             // registers); shared memory holds the count
-                             // and increment tables only then
+                             // registers; wider rows always); shared memory
+                             // holds the count and increment tables, or
+                             // the rings and gene tables, only then
+  int wpc;                   // warps per chain: 1 (blocks of one-warp
+                             // chains), or 2-4 (a block is one chain)
 };
 
 // Initial state of each chain: evaluate its tree at (alpha_mean,

@@ -525,7 +525,8 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   }
 }
 
-// One work unit of the batched launch: chain `chain` of dataset `d`.
+// One work unit of the batched launch: chain `chain` of dataset `d`, run
+// by the wpc warps of its slot (warp wic of them).
 template <int W32, int Q, bool SUM>
 __device__ __forceinline__ void batch_unit(const BatchArgs &b,
                                            const DatasetDev &ds,
@@ -533,14 +534,15 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
                                            uint32_t d, uint32_t *buf0,
                                            int *part, volatile int *sflag,
                                            uint4 *pbuf, const SlotSum &ss_in,
-                                           Cells<W32, Q> &cb, int lane) {
+                                           Cells<W32, Q> &cb, int wpc,
+                                           int wic, int lane) {
   constexpr int RS = rs_of_w32(W32);
   // the dataset's node count is within this launch's row width
   uint32_t *buf1 = buf0 + ds.n_nodes * RS;
   // rows of five to eight words stream their cells per evaluation (their
   // counts come through the ring and a gene table built per chunk)
-  const bool resident = W32 <= 4 && ds.n_cells <= 32 * Q;
-  if (resident) load_cells<W32, Q>(cb, ds, 0, 32, lane);
+  const bool resident = W32 <= 4 && ds.n_cells <= 32 * wpc * Q;
+  if (resident) load_cells<W32, Q>(cb, ds, 32 * wic, 32 * wpc, lane);
   const uint64_t off = b.chain_off[chain];
   // Philox key: the chain's number within its dataset, so a dataset's
   // chains draw the same moves here as in a one-dataset run.
@@ -551,11 +553,13 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
   run_chain<W32, Q, SUM>(ds, md, local, b.rows + off, b.best_rows + off,
                          nullptr, nullptr, 1, b.states + chain, nullptr,
                          nullptr, b.n_steps, b.cancel, b.status, buf0, buf1,
-                         part, sflag, pbuf, ss, cb, resident, 1, 0, lane);
+                         part, sflag, pbuf, ss, cb, resident, wpc, wic, lane);
 }
 
 // Many datasets: warps take chains from a shared work list (costliest
-// first); each chain brings its own dataset and rules.  One warp per chain.
+// first); each chain brings its own dataset and rules.  One warp per chain
+// (blocks of one-warp slots), or wpc warps per chain (the block is one
+// slot and takes its chains together).
 // Rows of five to eight words leave the register count free (up to 255):
 // a one-warp slot there takes about 31 KB of shared memory, so at most 7
 // such blocks fit an SM whatever their registers, and with the tighter
@@ -569,35 +573,53 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   constexpr int RS = rs_of_w32(W32);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  // one dataset in this launch with its cells in registers: inherited
-  // counts (the host's decision, the same in every thread)
+  const int wpc = b.wpc;
+  const int slot = wib / wpc, wic = wib - slot * wpc;
+  // inherited counts (the host's decision, the same in every thread)
   const bool counts = b.with_counts != 0;
   const bool scratch = SUM || counts;
-  const int sb = slot_bytes(b.max_nodes, RS, 1, scratch, W32, Q, counts);
-  uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)wib * sb;
+  const int sb = slot_bytes(b.max_nodes, RS, wpc, scratch, W32, Q, counts);
+  uint8_t *slot_base = reinterpret_cast<uint8_t *>(smem) + (size_t)slot * sb;
   uint32_t *buf0 = reinterpret_cast<uint32_t *>(slot_base);
   int *part = reinterpret_cast<int *>(buf0 + 2 * b.max_nodes * RS);
-  volatile int *sflag = part + 24;
+  volatile int *sflag = part + 24 * wpc;
+  // the slot's next unit, shared by its warps (the flag words' second)
+  volatile unsigned int *sunit =
+      reinterpret_cast<volatile unsigned int *>(sflag + 1);
   uint4 *pbuf = reinterpret_cast<uint4 *>(
-      slot_base + 4 * (2 * b.max_nodes * RS + 24 + 4));
+      slot_base + 4 * (2 * b.max_nodes * RS + 24 * wpc + 4) +
+      kPhiloxBytes * wic);
   SlotSum ss{};
   if (scratch) {
-    ss = slot_sum(slot_base, b.max_nodes, RS, 1, 0, W32, Q, counts);
+    ss = slot_sum(slot_base, b.max_nodes, RS, wpc, wic, W32, Q, counts);
     if constexpr (W32 <= 4) {
       if (counts) {
+        // one increment table per warp part of a chain (the launch's one
+        // dataset)
         uint8_t *table = reinterpret_cast<uint8_t *>(smem) +
-                         (size_t)(blockDim.x >> 5) * sb;
-        build_increments<Q>(table, 1, b.ds[b.table_ds], RS);
+                         (size_t)((blockDim.x >> 5) / wpc) * sb;
+        const DatasetDev &tds = b.ds[b.table_ds];
+        build_increments<Q>(table, wpc, tds, RS);
         __syncthreads();
-        ss.sx.inc = reinterpret_cast<const uint32_t *>(table);
+        ss.sx.inc = reinterpret_cast<const uint32_t *>(
+            table + (size_t)wic * inc_table_bytes(tds.n_nodes, Q));
       }
     }
   }
   Cells<W32, Q> cb;
   for (;;) {
     unsigned int unit = 0;
-    if (lane == 0) unit = atomicAdd(b.next_unit, 1u);
-    unit = __shfl_sync(BBS_FULL_MASK, unit, 0);
+    if (wpc == 1) {
+      if (lane == 0) unit = atomicAdd(b.next_unit, 1u);
+      unit = __shfl_sync(BBS_FULL_MASK, unit, 0);
+    } else {
+      // the block's warps take each unit together (the previous unit's
+      // reads of *sunit ended before the first barrier)
+      __syncthreads();
+      if (threadIdx.x == 0) *sunit = atomicAdd(b.next_unit, 1u);
+      __syncthreads();
+      unit = *sunit;
+    }
     if (unit >= (unsigned int)b.n_units) break;
     const uint32_t chain = b.units[unit];
     if (!device_check(chain < (uint32_t)b.n_chains, b.status, kCheckUnit, chain,
@@ -612,12 +634,12 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
     // (measured faster there).
     if constexpr (SUM) {
       batch_unit<W32, Q, SUM>(b, b.ds[d], b.md[d], chain, d, buf0, part,
-                              sflag, pbuf, ss, cb, lane);
+                              sflag, pbuf, ss, cb, wpc, wic, lane);
     } else {
       const DatasetDev ds = b.ds[d];
       const ModelDev md = b.md[d];
       batch_unit<W32, Q, SUM>(b, ds, md, chain, d, buf0, part, sflag, pbuf,
-                              ss, cb, lane);
+                              ss, cb, wpc, wic, lane);
     }
   }
 }

@@ -42,20 +42,24 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
   return (int)cudaGetLastError();
 }
 
-// Work-list launch: enough resident warps to fill the GPU, never more than
-// there are units.
+// Work-list launch: enough resident slots to fill the GPU, never more than
+// there are units.  Blocks of wpb one-warp slots (b.wpc == 1), or of one
+// slot of wpb == b.wpc warps.
 template <int W32, int Q, bool SUM>
 int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   const int threads = 32 * wpb;
   if (threads > chain_max_threads(Q)) return (int)cudaErrorInvalidConfiguration;
+  if (b.wpc < 1 || b.wpc > 4 || (b.wpc > 1 && wpb != b.wpc))
+    return (int)cudaErrorInvalidValue;
+  const int slots = wpb / b.wpc;
   const bool counts = b.with_counts != 0;
   if (counts && W32 <= 4 && b.table_ds < 0)
     return (int)cudaErrorInvalidValue;  // count tables need one dataset's rows
   const size_t smem =
-      (size_t)wpb * slot_bytes(b.max_nodes, RS, 1, SUM || counts, W32, Q,
-                               counts) +
-      table_bytes(b.max_nodes, W32, Q, 1, counts);
+      (size_t)slots * slot_bytes(b.max_nodes, RS, b.wpc, SUM || counts, W32,
+                                 Q, counts) +
+      table_bytes(b.max_nodes, W32, Q, b.wpc, counts);
   auto kern = batch_kernel<W32, Q, SUM>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
@@ -63,7 +67,7 @@ int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
   if (e != cudaSuccess) return (int)e;
   if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
-  const int want = (b.n_units + wpb - 1) / wpb;
+  const int want = (b.n_units + slots - 1) / slots;
   const int blocks = std::max(1, std::min(want, per_sm * n_sms));
   kern<<<blocks, threads, smem, s>>>(b);
   return (int)cudaGetLastError();

@@ -112,6 +112,8 @@ def lib():
         "bbs_batch_last_run_ms": (C.c_int, [v, v]),
         "bbs_batch_set_launch": (C.c_int, [v, C.c_int, C.c_int, C.c_int]),
         "bbs_batch_get_launch": (C.c_int, [v, v, v, v]),
+        "bbs_batch_set_chain_warps": (C.c_int, [v, C.c_int]),
+        "bbs_batch_get_chain_warps": (C.c_int, [v, v]),
         "bbs_batch_autotune": (C.c_int, [v, u32, v]),
         "bbs_batch_get_best": (C.c_int, [v, u32, v, v, v, v, v]),
         "bbs_batch_save_chains": (C.c_int, [v, v, v]),
@@ -474,6 +476,14 @@ class Batch:
         check(lib().bbs_batch_get_launch(self._h, C.byref(q), C.byref(w),
                                          C.byref(m)))
         return q.value, w.value, m.value
+
+    def set_chain_warps(self, warps_per_chain: int) -> None:
+        check(lib().bbs_batch_set_chain_warps(self._h, warps_per_chain))
+
+    def chain_warps(self) -> int:
+        w = C.c_int()
+        check(lib().bbs_batch_get_chain_warps(self._h, C.byref(w)))
+        return w.value
 
     def autotune(self, probe_steps: int = 64) -> float:
         ms = C.c_float()

@@ -81,7 +81,7 @@ def parse_args(argv=None):
                          "chains_per_block")
     ap.add_argument("--batch-launch", default="",
                     help="batched form: cells_per_lane,warps_per_block,"
-                         "merge_rows")
+                         "merge_rows[,warps_per_chain]")
     ap.add_argument("--mix-datasets", type=int, default=512)
     ap.add_argument("--mix-steps", type=int, default=20000,
                     help="512-dataset mix: steps per chain of the batched "
@@ -316,12 +316,12 @@ def run_reference(args) -> None:
 PROFILE = "chain_kernels_95x96.json"
 
 
-def _profile_figure(form: str, key: str):
-    """A figure of a chain kernel at the bench's shape from the committed
-    ncu summary profiles/chain_kernels_95x96.json (form "batch" or
+def _profile_figure(form: str, key: str, profile: str = PROFILE):
+    """A figure of a chain kernel from a committed ncu summary (by default
+    profiles/chain_kernels_95x96.json, the bench's shape; form "batch" or
     "plain"; warp instructions per chain-step, DRAM bytes per chain per
     launch), or None."""
-    p = os.path.join(ROOT, "profiles", PROFILE)
+    p = os.path.join(ROOT, "profiles", profile)
     if not os.path.exists(p):
         return None
     with open(p) as f:
@@ -417,7 +417,7 @@ def run_mix(N, n_datasets, chains, steps, flush, torch, tuned_steps=None):
         torch.cuda.synchronize()
         bt.run(steps)
         batched_ms = bt.last_run_ms()
-        shape = bt.launch()
+        shape = bt.launch() + (bt.chain_warps(),)
     plain_ms = tuned_ms = 0.0
     for i, ((mut, known, Cn, G), _, _) in enumerate(mix):
         with N.Context(mut, known, Cn, G, params[i]) as c:
@@ -442,7 +442,8 @@ def run_mix(N, n_datasets, chains, steps, flush, torch, tuned_steps=None):
             "pairs_per_chain_step": mix_pairs(mix),
             "batched_launch": {"cells_per_lane": shape[0],
                                "warps_per_block": shape[1],
-                               "merged_row_widths": bool(shape[2])}}
+                               "merged_row_widths": bool(shape[2]),
+                               "warps_per_chain": shape[3]}}
 
 
 def mix_pairs(mix) -> float:
@@ -581,14 +582,19 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
     }
 
 
+CAPS_PROFILE = "chain_kernels_255x512.json"
+
+
 def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
     """255 genes x 512 cells (alpha=5e-4, beta=0.25, 8% unknown, 1%
     homozygous): the batched form with the sum score and Langevin error
     moves against the plain form (max score, fixed rates), device time of
     one launch of `steps` steps after `warm` warm-up steps (the rate of the
     first few hundred steps from random trees is lower: the sum score sums
-    many cells twice while their best attachment lies far below the bound
-    it is taken against)."""
+    many cells a second time while their best attachment lies far below
+    the bound it is taken against).  Both forms inherit counts through the
+    ring (rows of eight words); the roofline is the issue slots, from the
+    warp instructions per chain-step of the committed ncu summary."""
     from bbscite_gb300 import data as D
     G, Cn = 255, 512
     m, _, _ = D.generate_dataset(5255, G, Cn, 5e-4, 0.25, 0.08, 0.01)
@@ -609,7 +615,7 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
         bt.run(steps)
         out["batched_adjoint_chain_steps_per_s"] = \
             chains * steps / (bt.last_run_ms() / 1e3)
-        out["batched_launch"] = list(bt.launch())
+        out["batched_launch"] = list(bt.launch()) + [bt.chain_warps()]
     with N.Context(mut, known, Cn, G, plain) as c:
         c.init_chains(chains)
         c.run(warm)
@@ -620,10 +626,33 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
         out["plain_chain_steps_per_s"] = \
             chains * steps / (c.last_run_ms() / 1e3)
         out["plain_launch"] = list(c.launch())
+    out["batched_over_plain"] = (out["batched_adjoint_chain_steps_per_s"]
+                                 / out["plain_chain_steps_per_s"])
     popc = popc_per_chain_step(G, Cn)
-    peak, _ = N.popc_peak()
+    peak, clk_hz = N.popc_peak()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    issue_peak = 4.0 * sms * clk_hz
+    inst_b = _profile_figure("batch", "warp_instructions_per_chain_step",
+                             CAPS_PROFILE)
+    inst_p = _profile_figure("plain", "warp_instructions_per_chain_step",
+                             CAPS_PROFILE)
+
+    def issue_frac(r, inst):
+        return None if inst is None else r * inst / issue_peak
+
+    out["roofline"] = {
+        "bound": "issue", "unit": "G warp-instructions/s",
+        "peak": issue_peak / 1e9,
+        "batched_adjoint_frac": issue_frac(
+            out["batched_adjoint_chain_steps_per_s"], inst_b),
+        "plain_frac": issue_frac(out["plain_chain_steps_per_s"], inst_p),
+        "batched_adjoint_work_per_chain_step": inst_b,
+        "plain_work_per_chain_step": inst_p,
+        "work_source": f"smsp__inst_executed.sum per chain-step of the "
+                       f"captured launch shapes, profiles/{CAPS_PROFILE}"}
+    # POPC-equivalent work (the masked-popcount formulation's count; the
+    # ring path issues none of these POPC)
     out["popc_per_chain_step"] = popc
-    # POPC-equivalent work (the masked-popcount formulation's count)
     out["batched_adjoint_popc_equivalent_frac"] = \
         out["batched_adjoint_chain_steps_per_s"] * popc / peak
     out["plain_popc_equivalent_frac"] = \
@@ -681,10 +710,13 @@ def run_ours(args) -> None:
     bt = N.Batch([(mut, known, Cn, G)], adj)
     bt.init_chains(chains)
     if args.batch_launch:
-        bt.set_launch(*[int(x) for x in args.batch_launch.split(",")])
+        v = [int(x) for x in args.batch_launch.split(",")]
+        bt.set_launch(*v[:3])
+        if len(v) > 3:
+            bt.set_chain_warps(v[3])
     elif args.autotune:
         bt.autotune(args.autotune_steps)
-    bshape = bt.launch()
+    bshape = bt.launch() + (bt.chain_warps(),)
     ctx = N.Context(mut, known, Cn, G, plain)
     ctx.init_chains(chains)
     if args.launch:
@@ -778,7 +810,8 @@ def run_ours(args) -> None:
         t = time.perf_counter()
         b2 = N.Batch([(mut, known, Cn, G)], adj)
         b2.init_chains(chains)
-        b2.set_launch(*bshape)
+        b2.set_launch(*bshape[:3])
+        b2.set_chain_warps(bshape[3])
         b2.run(L)
         b2.best(0)
         b2.close()
@@ -819,6 +852,7 @@ def run_ours(args) -> None:
             "chain_steps_per_launch": L, "parallelism": f"replicas x{ws}",
             "launch": {"cells_per_lane": bshape[0],
                        "warps_per_block": bshape[1],
+                       "warps_per_chain": bshape[3],
                        "autotuned": bool(args.autotune) and not args.batch_launch},
             "l2": "256 MiB buffer written between launches",
         },
@@ -884,6 +918,10 @@ def run_ours(args) -> None:
         "caps_batched_adjoint":
             caps["batched_adjoint_chain_steps_per_s"] if caps else None,
         "caps_plain": caps["plain_chain_steps_per_s"] if caps else None,
+        "caps_batched_issue_frac":
+            caps["roofline"]["batched_adjoint_frac"] if caps else None,
+        "caps_plain_issue_frac":
+            caps["roofline"]["plain_frac"] if caps else None,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

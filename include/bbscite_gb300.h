@@ -325,8 +325,17 @@ BBS_API int bbs_batch_set_launch(bbs_batch *batch, int cells_per_lane,
                                  int warps_per_block, int merge_rows);
 BBS_API int bbs_batch_get_launch(const bbs_batch *batch, int *cells_per_lane,
                                  int *warps_per_block, int *merge_rows);
-/* Times probe_steps steps per launch shape (chain states restored) and
- * keeps the fastest. */
+/* Chain-to-warp mapping: 1 (default) runs each chain on one warp, in
+ * blocks of warps_per_block chains; 2-4 splits each chain's cells over that
+ * many warps, one chain per block (warps_per_block is then ignored).
+ * Chains are bit-identical under every mapping. */
+BBS_API int bbs_batch_set_chain_warps(bbs_batch *batch, int warps_per_chain);
+BBS_API int bbs_batch_get_chain_warps(const bbs_batch *batch,
+                                      int *warps_per_chain);
+/* Times probe_steps steps per launch shape -- cells per lane, one-warp
+ * chains in blocks of 1, 2, 4, 7 or 8, or chains of 2 or 4 warps, with and
+ * without merged row widths (chain states restored) -- and keeps the
+ * fastest. */
 BBS_API int bbs_batch_autotune(bbs_batch *batch, uint32_t probe_steps,
                                float *best_ms);
 /* Best proposal of one dataset (over its chains). */

@@ -78,6 +78,8 @@ bool check(int n, int q, int wpc, int cpb, bool sum, bool counts) {
     if ((sum ? part + psum : part + pmax) > flag)
       return fail("partials overrun the flag", n, q, wpc, cpb, sum, "");
     all.push_back({"flag", flag, flag + 4, 4});
+    // the batched kernel's unit word of a multi-warp slot
+    all.push_back({"unit", flag + 4, flag + 8, 4});
     // each warp's Philox blocks (32 x 16 bytes) after the flag words
     for (int wic = 0; wic < wpc; wic++) {
       const size_t ph = flag + 16 + (size_t)bbs::kPhiloxBytes * wic;
@@ -160,8 +162,8 @@ int main() {
           for (int wpc = 2; wpc <= 4; wpc++)
             if (!check(n, q, wpc, 1, sum != 0, counts != 0)) return 1;
         }
-  // (the batched kernel's launches are one-warp slots, 1..8 per block: the
-  // cases of the plain kernel with wpc = 1)
+  // (the batched kernel's launches are one-warp slots, 1..8 per block, or
+  // one slot of 2..4 warps: the cases of the plain kernel)
   std::printf("layout ok %ld\n", g_cases);
   return 0;
 }

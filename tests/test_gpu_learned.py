@@ -229,8 +229,9 @@ def test_batch_equals_single_dataset_runs(native, score, move):
 @pytest.mark.parametrize("score", ["max", "sum"])
 def test_batch_autotune_and_shapes_agree(native, score):
     """Every launch shape of the batched form -- cells per lane, warps per
-    block, merged row widths -- and the tuned one give the same chains, and
-    every chain of every launch group runs all its steps."""
+    block, merged row widths, one-warp chains or chains of 2 and 4 warps --
+    and the tuned one give the same chains, and every chain of every launch
+    group runs all its steps."""
     # every row width of up to four words with 1-4 groups of 32 cells, and
     # two wider datasets
     specs = [(G, Cn) for G in (20, 50, 80, 110) for Cn in (20, 50, 80, 110)]
@@ -246,14 +247,18 @@ def test_batch_autotune_and_shapes_agree(native, score):
     else:
         p = _headline_params(native, seed=3)
     results = []
-    for shape in ((1, 1, 0), (2, 4, 0), (4, 2, 1), (3, 8, 0), (4, 7, 1),
+    # (cells per lane, warps per block, merged widths, warps per chain)
+    for shape in ((1, 1, 0, 1), (2, 4, 0, 1), (4, 2, 1, 1), (3, 8, 0, 1),
+                  (4, 7, 1, 1), (2, 0, 0, 2), (1, 0, 1, 4), (3, 0, 0, 4),
                   None):
         with native.Batch(datasets, p) as b:
             b.init_chains(4)
             if shape is None:
                 assert b.autotune(40) > 0
             else:
-                b.set_launch(*shape)
+                b.set_launch(*shape[:3])
+                b.set_chain_warps(shape[3])
+                assert b.chain_warps() == shape[3]
             b.run(150)
             img = b.save_chains()
             # every chain ran: its state (128 bytes, at the image's end)
@@ -396,12 +401,14 @@ def test_wide_row_ring_chains_replay_in_fp64(native, orc, G, Cn, launch):
                       final["dm"][ch]) <= 2
 
 
-def test_headline_batch_equals_replayed_chains(native, orc):
+@pytest.mark.parametrize("wpc", [1, 2])
+def test_headline_batch_equals_replayed_chains(native, orc, wpc):
     """The batched launch of the bench's headline shape -- one 95 x 96
-    dataset, 3 cells per lane, 4-warp blocks, the dataset's increment table
-    built in the block -- leaves every chain (rows, best proposal and
-    state) bit-identical to the same chains run alone with a trace, and
-    those traced chains replay step by step in FP64."""
+    dataset, 3 cells per lane, 4-warp blocks of one-warp chains (or chains
+    of 2 warps, one per block), the dataset's increment tables built in the
+    block -- leaves every chain (rows, best proposal and state)
+    bit-identical to the same chains run alone with a trace, and those
+    traced chains replay step by step in FP64."""
     G, Cn = 95, 96
     m, _, _ = D.generate_dataset(2026, G, Cn, 1e-3, 0.2, 0.1, 0.02)
     mut, known = D.matrix_to_bits(m)
@@ -410,7 +417,8 @@ def test_headline_batch_equals_replayed_chains(native, orc):
     with native.Batch([(mut, known, Cn, G)], p) as b:
         b.init_chains(chains)
         b.set_launch(3, 4, 0)
-        assert b.launch()[:2] == (3, 4)
+        b.set_chain_warps(wpc)
+        assert b.launch()[:2] == (3, 4) and b.chain_warps() == wpc
         b.run(steps)
         img_b = b.save_chains()
     with native.Context(mut, known, Cn, G, p) as c:
