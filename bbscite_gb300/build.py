@@ -40,7 +40,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
               "-I" + CSRC]
 UNITS = ["bbs_mcmc_lo.cu", "bbs_mcmc_lo_rec.cu", "bbs_mcmc_hi.cu",
          "bbs_mcmc_hi_rec.cu", "bbs_aux.cu", "bbs_api.cu",
-         "bbs_batch.cu"]
+         "bbs_batch.cu", "bbs_batch_multi.cu"]
 
 
 def nvcc() -> str:

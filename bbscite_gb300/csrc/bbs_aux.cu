@@ -26,6 +26,9 @@ int launch_mcmc(const RunArgs &a, int q, int cpb, int n_sms, void *stream) {
 int launch_batch(const BatchArgs &b, int w32, int q, bool sum, int wpb,
                  int n_sms, void *stream) {
   cudaStream_t s = (cudaStream_t)stream;
+  if (b.wpc > 1)
+    return w32 <= 4 ? launch_batch_lo_multi(b, w32, q, sum, wpb, n_sms, s)
+                    : launch_batch_hi_multi(b, w32, q, sum, wpb, n_sms, s);
   if (w32 <= 4) return launch_batch_lo(b, w32, q, sum, wpb, n_sms, s);
   return launch_batch_hi(b, w32, q, sum, wpb, n_sms, s);
 }

@@ -565,7 +565,9 @@ __device__ __forceinline__ void batch_unit(const BatchArgs &b,
 // such blocks fit an SM whatever their registers, and with the tighter
 // bound of two cells per lane (168) the sum score's kernel spilled
 // (measured at 255 x 512: 7.5 M against 6.7 M chain-steps/s).
-template <int W32, int Q, bool SUM>
+// MULTI: chains of b.wpc > 1 warps; without it every chain is one warp,
+// known at compile time.
+template <int W32, int Q, bool SUM, bool MULTI>
 __global__ void __launch_bounds__(ChainBounds<Q>::threads,
                                   W32 > 4 ? 1 : ChainBounds<Q>::min_blocks)
     batch_kernel(const BatchArgs b) {
@@ -573,7 +575,7 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   constexpr int RS = rs_of_w32(W32);
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int wpc = b.wpc;
+  const int wpc = MULTI ? b.wpc : 1;
   const int slot = wib / wpc, wic = wib - slot * wpc;
   // inherited counts (the host's decision, the same in every thread)
   const bool counts = b.with_counts != 0;
@@ -609,7 +611,7 @@ __global__ void __launch_bounds__(ChainBounds<Q>::threads,
   Cells<W32, Q> cb;
   for (;;) {
     unsigned int unit = 0;
-    if (wpc == 1) {
+    if constexpr (!MULTI) {
       if (lane == 0) unit = atomicAdd(b.next_unit, 1u);
       unit = __shfl_sync(BBS_FULL_MASK, unit, 0);
     } else {

@@ -45,12 +45,13 @@ int launch_mcmc_t(const RunArgs &a, int cpb, int n_sms, cudaStream_t s) {
 // Work-list launch: enough resident slots to fill the GPU, never more than
 // there are units.  Blocks of wpb one-warp slots (b.wpc == 1), or of one
 // slot of wpb == b.wpc warps.
-template <int W32, int Q, bool SUM>
+template <int W32, int Q, bool SUM, bool MULTI>
 int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
   constexpr int RS = rs_of_w32(W32);
   const int threads = 32 * wpb;
   if (threads > chain_max_threads(Q)) return (int)cudaErrorInvalidConfiguration;
-  if (b.wpc < 1 || b.wpc > 4 || (b.wpc > 1 && wpb != b.wpc))
+  if (b.wpc < 1 || b.wpc > 4 || (b.wpc > 1) != MULTI ||
+      (MULTI && wpb != b.wpc))
     return (int)cudaErrorInvalidValue;
   const int slots = wpb / b.wpc;
   const bool counts = b.with_counts != 0;
@@ -60,7 +61,7 @@ int launch_batch_t(const BatchArgs &b, int wpb, int n_sms, cudaStream_t s) {
       (size_t)slots * slot_bytes(b.max_nodes, RS, b.wpc, SUM || counts, W32,
                                  Q, counts) +
       table_bytes(b.max_nodes, W32, Q, b.wpc, counts);
-  auto kern = batch_kernel<W32, Q, SUM>;
+  auto kern = batch_kernel<W32, Q, SUM, MULTI>;
   cudaError_t e = prepare_smem(kern, smem);
   if (e != cudaSuccess) return (int)e;
   int per_sm = 0;
@@ -86,5 +87,10 @@ int launch_batch_lo(const BatchArgs &b, int w32, int q, bool sum, int wpb,
                     int n_sms, cudaStream_t s);
 int launch_batch_hi(const BatchArgs &b, int w32, int q, bool sum, int wpb,
                     int n_sms, cudaStream_t s);
+// (chains of several warps: their own units)
+int launch_batch_lo_multi(const BatchArgs &b, int w32, int q, bool sum,
+                          int wpb, int n_sms, cudaStream_t s);
+int launch_batch_hi_multi(const BatchArgs &b, int w32, int q, bool sum,
+                          int wpb, int n_sms, cudaStream_t s);
 
 }  // namespace bbs

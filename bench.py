@@ -97,6 +97,12 @@ def parse_args(argv=None):
     ap.add_argument("--caps-steps", type=int, default=500,
                     help="255x512 run: steps per launch (0: off)")
     ap.add_argument("--caps-chains", type=int, default=4096)
+    ap.add_argument("--caps-profile", default="", choices=["", "batch", "plain"],
+                    help="only the 255x512 kernel of one form at the shape "
+                         "its tuner picks (batched: 2 cells per lane, chains "
+                         "of 2 warps; plain: 2 cells per lane, chains of 4 "
+                         "warps), one 1500-step launch and one 100-step "
+                         "launch, for an ncu capture of the second")
     return ap.parse_args(argv)
 
 
@@ -660,6 +666,38 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
     return out
 
 
+def caps_profile(form: str, chains: int = 4096) -> None:
+    """The 255x512 case of run_beyond_caps for an ncu capture: one form at
+    a fixed launch shape, a 1500-step launch, then the 100-step launch to
+    capture."""
+    from bbscite_gb300 import data as D
+    from bbscite_gb300 import native as N
+    G, Cn = 255, 512
+    m, _, _ = D.generate_dataset(5255, G, Cn, 5e-4, 0.25, 0.08, 0.01)
+    mut, known = D.matrix_to_bits(m)
+    steps = 100
+    if form == "batch":
+        p = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5,
+                             prob_beta_change=0.1, score_mode=N.SCORE_SUM,
+                             error_move=N.ERROR_LANGEVIN)
+        with N.Batch([(mut, known, Cn, G)], p) as bt:
+            bt.init_chains(chains)
+            bt.set_launch(2, 2, 1)
+            bt.set_chain_warps(2)
+            bt.run(1500)
+            bt.run(steps)
+            rate = chains * steps / (bt.last_run_ms() / 1e3)
+    else:
+        p = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5)
+        with N.Context(mut, known, Cn, G, p) as c:
+            c.init_chains(chains)
+            c.set_launch(2, 4, 1)
+            c.run(1500)
+            c.run(steps)
+            rate = chains * steps / (c.last_run_ms() / 1e3)
+    print(json.dumps({"caps_profile": form, "chain_steps_per_s": rate}))
+
+
 def own_gpu(local: int) -> str:
     """Makes this rank's GPU the only visible one, before any CUDA call, so
     that torch and the library (which links its own CUDA runtime) both use
@@ -714,16 +752,10 @@ def run_ours(args) -> None:
         bt.set_launch(*v[:3])
         if len(v) > 3:
             bt.set_chain_warps(v[3])
-    elif args.autotune:
-        bt.autotune(args.autotune_steps)
-    bshape = bt.launch() + (bt.chain_warps(),)
     ctx = N.Context(mut, known, Cn, G, plain)
     ctx.init_chains(chains)
     if args.launch:
         ctx.set_launch(*[int(x) for x in args.launch.split(",")])
-    elif args.autotune:
-        ctx.autotune(args.autotune_steps)
-    pshape = ctx.launch()
 
     done = 0
     while done < args.quality_steps:
@@ -731,6 +763,15 @@ def run_ours(args) -> None:
         bt.run(k)
         ctx.run(k)
         done += k
+    # launch shapes tuned on the warmed-up chains, the regime timed (the
+    # tuners restore the chains' states; every shape computes the same
+    # chains)
+    if args.autotune and not args.batch_launch:
+        bt.autotune(args.autotune_steps)
+    if args.autotune and not args.launch:
+        ctx.autotune(args.autotune_steps)
+    bshape = bt.launch() + (bt.chain_warps(),)
+    pshape = ctx.launch()
     for _ in range(args.warmup):
         bt.run(L)
         ctx.run(L)
@@ -933,6 +974,8 @@ def main(argv=None) -> None:
     args = parse_args(argv)
     if args.impl == "reference":
         run_reference(args)
+    elif args.caps_profile:
+        caps_profile(args.caps_profile, args.caps_chains)
     else:
         run_ours(args)
 

@@ -249,9 +249,12 @@ def test_mcmc_replay_golden(native, orc, golden):
         tr = _replay_check(native, orc, golden[f"chain{ci}_matrix"], 1e-3,
                            0.2, [golden[f"chain{ci}_start"]], raw,
                            exact_scores=(p_beta == 0))
-        # the reference's own decisions agree outside the float band
+        # the reference's own recorded decisions (its cell-order score):
+        # the class-total chains make every one of them (measured: all
+        # 5,100 steps of the four chains); at most the replay's one
+        # decision inside the rounding band may differ
         ref_acc = golden[f"chain{ci}_accepted"]
-        assert (tr["accepted"][0] != ref_acc).mean() < 0.01
+        assert int((tr["accepted"][0] != ref_acc).sum()) <= 1
 
 
 @pytest.mark.parametrize("G,Cn,chains", [(16, 20, 7), (63, 64, 5),

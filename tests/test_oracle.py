@@ -190,6 +190,25 @@ def test_golden_chain_class_total_scores(orc, golden):
                 golden[f"chain{ci}_final_parent"]).all()
 
 
+def test_golden_chains_run_free_make_every_reference_decision(orc, golden):
+    """Run free on the reference's recorded moves (no decision forced), the
+    class-total chains make the reference's own decision -- taken on its
+    cell-order score -- at every one of the 5,100 steps of the four golden
+    chains, and end on its trees."""
+    total = 0
+    for ci, (G, Cn, steps, _) in enumerate(golden["chain_cases"]):
+        mut, known = D.matrix_to_bits(golden[f"chain{ci}_matrix"])
+        res = orc.run_chain(1e-3, 0.2, 0.1, 1.0, golden[f"chain{ci}_start"],
+                            mut, known, golden[f"chain{ci}_raw"],
+                            score_mode=1)
+        acc = res["trace"]["accepted"]
+        assert (acc == golden[f"chain{ci}_accepted"]).all()
+        assert (orc.parent_vector(res["dm"]) ==
+                golden[f"chain{ci}_final_parent"]).all()
+        total += len(acc)
+    assert total == 5100
+
+
 # ------------------------------------------------------------- fuzzing --
 
 def _parent_vector_move(pv, mp, am):
