@@ -101,7 +101,7 @@ def parse_args(argv=None):
                     help="only the 255x512 kernel of one form at the shape "
                          "its tuner picks (batched: 2 cells per lane, chains "
                          "of 2 warps; plain: 2 cells per lane, chains of 4 "
-                         "warps), one 1500-step launch and one 100-step "
+                         "warps), one 20,000-step launch and one 100-step "
                          "launch, for an ncu capture of the second")
     return ap.parse_args(argv)
 
@@ -591,16 +591,18 @@ def run_langevin_vs_rw(N, mut, known, G, Cn, chains, total, seeds,
 CAPS_PROFILE = "chain_kernels_255x512.json"
 
 
-def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
+def run_beyond_caps(N, chains, steps, flush, torch, warm=20000, early=1500):
     """255 genes x 512 cells (alpha=5e-4, beta=0.25, 8% unknown, 1%
     homozygous): the batched form with the sum score and Langevin error
     moves against the plain form (max score, fixed rates), device time of
-    one launch of `steps` steps after `warm` warm-up steps (the rate of the
-    first few hundred steps from random trees is lower: the sum score sums
-    many cells a second time while their best attachment lies far below
-    the bound it is taken against).  Both forms inherit counts through the
-    ring (rows of eight words); the roofline is the issue slots, from the
-    warp instructions per chain-step of the committed ncu summary."""
+    one launch of `steps` steps after `warm` steps from random trees: the
+    regime of nearly all of a 1,000,000-step run.  The rate after `early`
+    steps is reported too: there the sum score still sums many cells a
+    second time, while their best attachment lies far below the bound it is
+    taken against.  Launch shapes are tuned after `early` steps.  Both
+    forms inherit counts through the ring (rows of eight words); the
+    roofline is the issue slots, from the warp instructions per chain-step
+    of the committed ncu summary (captured after `warm` steps)."""
     from bbscite_gb300 import data as D
     G, Cn = 255, 512
     m, _, _ = D.generate_dataset(5255, G, Cn, 5e-4, 0.25, 0.08, 0.01)
@@ -610,27 +612,31 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
                            error_move=N.ERROR_LANGEVIN)
     plain = N.default_params(alpha_mean=5e-4, beta_mean=0.25, seed=5)
     out = {"n_genes": G, "n_cells": Cn, "chains": chains, "steps": steps,
-           "warm_up_steps": warm}
-    # launch shapes are tuned on the warmed-up chains, the regime timed
-    with N.Batch([(mut, known, Cn, G)], adj) as bt:
-        bt.init_chains(chains)
-        bt.run(warm)
-        bt.autotune(max(8, steps // 4))
+           "warm_up_steps": warm, "early_steps": early}
+
+    def timed(run, last_ms):
         flush.zero_()
         torch.cuda.synchronize()
-        bt.run(steps)
-        out["batched_adjoint_chain_steps_per_s"] = \
-            chains * steps / (bt.last_run_ms() / 1e3)
+        run(steps)
+        return chains * steps / (last_ms() / 1e3)
+
+    with N.Batch([(mut, known, Cn, G)], adj) as bt:
+        bt.init_chains(chains)
+        bt.run(early)
+        bt.autotune(max(8, steps // 4))
+        out["batched_adjoint_after_early_steps"] = timed(bt.run,
+                                                         bt.last_run_ms)
+        bt.run(warm - early - steps)
+        out["batched_adjoint_chain_steps_per_s"] = timed(bt.run,
+                                                         bt.last_run_ms)
         out["batched_launch"] = list(bt.launch()) + [bt.chain_warps()]
     with N.Context(mut, known, Cn, G, plain) as c:
         c.init_chains(chains)
-        c.run(warm)
+        c.run(early)
         c.autotune(max(8, steps // 4))
-        flush.zero_()
-        torch.cuda.synchronize()
-        c.run(steps)
-        out["plain_chain_steps_per_s"] = \
-            chains * steps / (c.last_run_ms() / 1e3)
+        out["plain_after_early_steps"] = timed(c.run, c.last_run_ms)
+        c.run(warm - early - steps)
+        out["plain_chain_steps_per_s"] = timed(c.run, c.last_run_ms)
         out["plain_launch"] = list(c.launch())
     out["batched_over_plain"] = (out["batched_adjoint_chain_steps_per_s"]
                                  / out["plain_chain_steps_per_s"])
@@ -668,8 +674,8 @@ def run_beyond_caps(N, chains, steps, flush, torch, warm=1500):
 
 def caps_profile(form: str, chains: int = 4096) -> None:
     """The 255x512 case of run_beyond_caps for an ncu capture: one form at
-    a fixed launch shape, a 1500-step launch, then the 100-step launch to
-    capture."""
+    a fixed launch shape, a 20,000-step launch (the timed regime), then the
+    100-step launch to capture."""
     from bbscite_gb300 import data as D
     from bbscite_gb300 import native as N
     G, Cn = 255, 512
@@ -684,7 +690,7 @@ def caps_profile(form: str, chains: int = 4096) -> None:
             bt.init_chains(chains)
             bt.set_launch(2, 2, 1)
             bt.set_chain_warps(2)
-            bt.run(1500)
+            bt.run(20000)
             bt.run(steps)
             rate = chains * steps / (bt.last_run_ms() / 1e3)
     else:
@@ -692,7 +698,7 @@ def caps_profile(form: str, chains: int = 4096) -> None:
         with N.Context(mut, known, Cn, G, p) as c:
             c.init_chains(chains)
             c.set_launch(2, 4, 1)
-            c.run(1500)
+            c.run(20000)
             c.run(steps)
             rate = chains * steps / (c.last_run_ms() / 1e3)
     print(json.dumps({"caps_profile": form, "chain_steps_per_s": rate}))
@@ -959,6 +965,7 @@ def run_ours(args) -> None:
         "caps_batched_adjoint":
             caps["batched_adjoint_chain_steps_per_s"] if caps else None,
         "caps_plain": caps["plain_chain_steps_per_s"] if caps else None,
+        "caps_batched_over_plain": caps["batched_over_plain"] if caps else None,
         "caps_batched_issue_frac":
             caps["roofline"]["batched_adjoint_frac"] if caps else None,
         "caps_plain_issue_frac":
