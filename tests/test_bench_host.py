@@ -48,3 +48,24 @@ def test_work_per_chain_step():
     assert bench.popc_per_chain_step(255, 512) == 2097152
     # the paper's counted bits, 4 * cells * nodes^2
     assert bench.counted_bits_per_chain_step(95, 96) == 4 * 96 * 96 ** 2
+
+
+def test_profile_figures_the_bench_reads():
+    """The committed ncu summaries give the warp instructions per chain-step
+    that turn each timed rate into an issue-slot fraction: the 95 x 96
+    kernels of the headline and the 255 x 512 kernels (the shapes and the
+    regime the bench times)."""
+    import bench
+    for form in ("batch", "plain"):
+        for prof in (bench.PROFILE, bench.CAPS_PROFILE):
+            w = bench._profile_figure(form, "warp_instructions", prof)
+            cs = bench._profile_figure(form, "chain_steps", prof)
+            per = bench._profile_figure(form,
+                                        "warp_instructions_per_chain_step",
+                                        prof)
+            assert isinstance(per, int) and per > 0, (form, prof)
+            assert abs(w / cs - per) <= 1, (form, prof)
+    # 95 x 96: 1024 chains x 2000 steps; 255 x 512: 4096 chains x 100 steps
+    assert bench._profile_figure("batch", "chain_steps") == 1024 * 2000
+    assert bench._profile_figure("batch", "chain_steps",
+                                 bench.CAPS_PROFILE) == 4096 * 100
