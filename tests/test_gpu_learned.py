@@ -195,10 +195,13 @@ def test_init_scores_match_fp64(native, orc, score):
                                         ("sum", "langevin")])
 def test_batch_equals_single_dataset_runs(native, score, move):
     """A dataset's chains in the batched launch are bit-identical to the
-    same chains run alone (same Philox keys, same kernel code)."""
+    same chains run alone (same Philox keys, same kernel code).  The two
+    datasets of 200 and 220 genes share a launch group (rows of seven
+    words), whose warps build their gene tables from either dataset's
+    cells."""
     rng = np.random.default_rng(9)
     specs = [(int(rng.integers(16, 128)), int(rng.integers(16, 200)))
-             for _ in range(7)] + [(200, 40), (33, 300)]
+             for _ in range(7)] + [(200, 40), (33, 300), (220, 100)]
     datasets, params = [], []
     for i, (G, Cn) in enumerate(specs):
         m, _, _ = D.generate_dataset(300 + i, G, Cn, 1e-3, 0.2, 0.1, 0.0)

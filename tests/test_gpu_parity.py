@@ -271,7 +271,9 @@ def test_mcmc_replay_random(native, orc, G, Cn, chains):
     _replay_check(native, orc, m, 1e-3, 0.2, starts, raws)
 
 
-@pytest.mark.parametrize("G,Cn,launch", [(200, 150, (1, 1, 3)),
+@pytest.mark.parametrize("G,Cn,launch", [(130, 100, (2, 1, 2)),
+                                         (170, 120, (1, 2, 1)),
+                                         (200, 150, (1, 1, 3)),
                                          (255, 300, (2, 1, 2)),
                                          (255, 300, (2, 3, 1))])
 def test_wide_rows_replay_with_stars_and_node0_fallbacks(native, orc, G, Cn,
@@ -283,7 +285,8 @@ def test_wide_rows_replay_with_stars_and_node0_fallbacks(native, orc, G, Cn,
     whose k-th (non)descendant falls back to node 0 (u = 1.0: those
     proposals' parent vectors are checked against their rows), replay bit
     for bit against the oracle: decisions, class counts, scores and final
-    rows, with one and with several warps per chain."""
+    rows, with one and with several warps per chain, at rows of five to
+    eight words (131 to 256 nodes)."""
     rng = np.random.default_rng(G * 7 + Cn)
     m, _, _ = D.generate_dataset(G + Cn, G, Cn, 1e-3, 0.2, 0.1, 0.02)
     mp = orc.move_probs(0.0, 0.55, 0.4, 0.05)
