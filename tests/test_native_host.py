@@ -222,3 +222,38 @@ def test_product_code_never_reaches_the_oracle():
                     text = f.read()
                 assert not re.search(r'#include\s+[<"][^">]*oracle', text), path
                 assert "libbbs_oracle" not in text and "liboracle" not in text, path
+
+
+def _ring_distance(parent: np.ndarray) -> int:
+    """The largest distance, in the canonical order (depth, then node
+    index), from a node back to its parent: the ring of counts that rows of
+    five to eight words inherit through must hold at least this many
+    positions."""
+    n = len(parent)
+    root = n - 1
+    depth = np.zeros(n, dtype=np.int64)
+    for x in range(n):
+        y, d = x, 0
+        while y != root:
+            y, d = int(parent[y]), d + 1
+        depth[x] = d
+    order = np.lexsort((np.arange(n), depth))
+    pos = np.empty(n, dtype=np.int64)
+    pos[order] = np.arange(n)
+    return int(max(pos[x] - pos[parent[x]] for x in range(n) if x != root))
+
+
+def test_random_trees_fit_the_ring():
+    """Random trees of 131 to 256 nodes (uniform Pruefer codes, the chains'
+    initial trees) fit the 64-entry ring: every node lies fewer than 64
+    positions after its parent in the canonical order, so their counts are
+    inherited without the masked-popcount fallback.  A star (every gene a
+    child of the root) does not fit, and falls back."""
+    rng = np.random.default_rng(2026)
+    worst = 0
+    for G in (130, 160, 200, 255):
+        for _ in range(60):
+            worst = max(worst, _ring_distance(D.random_parent_vector(rng, G)))
+    assert worst < 64, worst
+    star = np.full(256, 255, dtype=np.int64)
+    assert _ring_distance(star) >= 64
