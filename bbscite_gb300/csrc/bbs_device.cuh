@@ -1177,7 +1177,13 @@ __device__ __forceinline__ void inherit_one(const SumCtx &sx, int i, int lane,
 // inherit_pair for rows of five to eight words: the parents' counts come
 // from the ring (entries hold the parents' order positions, ring_order),
 // the increments from the gene table, and positions i and i + 1 are stored
-// in the ring.
+// in the ring.  Why no load reads an overwritten entry: when the loads run,
+// positions up to i - 1 are stored (each lane reads and writes only its own
+// column, in program order).  A parent at position p < i was stored at
+// entry p % kRing, and the positions stored since, p + 1 .. i - 1, are
+// fewer than kRing (ring_order checked i + 1 - p < kRing), so none of them
+// maps to that entry.  A parent at position i, not stored yet, is taken
+// from the register.
 template <int Q, int NW = kPackWords<Q>>
 __device__ __forceinline__ void inherit_pair_ring(const SumCtx &sx, int i,
                                                   int lane,
