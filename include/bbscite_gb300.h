@@ -319,8 +319,9 @@ BBS_API int bbs_batch_last_run_ms(const bbs_batch *batch, float *ms);
  * block (1-8; a launch group with 1-2 cells per lane takes at most 4, and
  * a block too large for its shared memory fails the run with
  * BBS_ERR_SIZE);
- * merge_rows != 0 runs 1- and 3-word trees with their 2- and 4-word row
- * stride group (one launch per group instead of two). */
+ * merge_rows != 0 runs trees of an odd number of 32-bit row words (1, 3,
+ * 5, 7) with the next even width, which has the same row stride (one
+ * launch per pair of widths instead of two). */
 BBS_API int bbs_batch_set_launch(bbs_batch *batch, int cells_per_lane,
                                  int warps_per_block, int merge_rows);
 BBS_API int bbs_batch_get_launch(const bbs_batch *batch, int *cells_per_lane,
